@@ -1,0 +1,21 @@
+"""Helpers shared by the test modules (tolerances follow the reference)."""
+import numpy as np
+
+# tests/rpp/cpu/single_thread/ops/cpu_typed_ft_ops_test_helper.hpp:33-36 and
+# :261-273: |a - e| <= tol * max(1, |a|, |e|), 1e-12 for double, 1e-5 for float.
+TOL_F64 = 1e-12
+TOL_F32 = 1e-5
+
+
+def rel_err(actual, expected):
+    actual = np.asarray(actual, dtype=np.float64)
+    expected = np.asarray(expected, dtype=np.float64)
+    if actual.size == 0:
+        return 0.0
+    scale = np.maximum(1.0, np.maximum(np.abs(actual), np.abs(expected)))
+    return float(np.max(np.abs(actual - expected) / scale))
+
+
+def assert_close(actual, expected, tol=TOL_F64, what=""):
+    e = rel_err(actual, expected)
+    assert np.isfinite(e) and e <= tol, f"{what}: relative error {e:.3e} > {tol:.1e}"
