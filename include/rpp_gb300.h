@@ -1,0 +1,265 @@
+/*
+ * rpp_gb300.h -- C ABI of the GB300-native (sm_103a) batched free-tensor
+ * library.  Plain pointers and sizes only: no CUDA, C++ or torch types cross
+ * this boundary, so a ctypes / cgo / JNI caller binds it directly.
+ *
+ * The entry points are what RoughPathPrimitives' operation API calls through a
+ * new `gpu` strategy (rpp::gpu::strategies::GB300Strategy, in the package's
+ * include/rpp/gpu/gb300/strategy.hpp).  Each declaration names the reference
+ * operation it replaces (paths relative to the reference project's root).
+ *
+ * Conventions (shared by every entry point):
+ *  - Status codes are the reference's rpp::ErrorCode values
+ *    (include/rpp/support/error.hpp:28-39); 0 is success.  The message of the
+ *    last failure on the calling host thread is rpp_gb_last_error_string().
+ *  - All tensor data pointers are DEVICE pointers.  A batch operand is
+ *    {data, stride, min_degree, max_degree}: batch element b is the dense
+ *    tensor at data + b*stride (elements, not bytes), coefficients in the
+ *    graded lexicographic order of include/rpp/basis/tensor_basis.hpp; the
+ *    degree range is the view's (include/rpp/views/dense_graded_vector_view.hpp):
+ *    coefficients outside it read as zero and are never written.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *    asynchronous and stream-ordered; none synchronises the device and none
+ *    allocates device memory after its plan / matrix handle is created.
+ *  - dtype selects the scalar and accumulation type: RPP_GB_F32 (float data,
+ *    float accumulation) or RPP_GB_F64 (double, double).
+ */
+#ifndef RPP_GB300_H
+#define RPP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* rpp::ErrorCode (include/rpp/support/error.hpp:28-39) */
+enum rpp_gb_status {
+    RPP_GB_SUCCESS = 0,
+    RPP_GB_CANCELLED = 1,
+    RPP_GB_UNKNOWN = 2,
+    RPP_GB_INVALID_ARGUMENT = 3,
+    RPP_GB_TIMEOUT = 4,
+    RPP_GB_OUT_OF_RESOURCES = 5,
+    RPP_GB_CONTRACT_VIOLATION = 6,
+    RPP_GB_OUT_OF_BOUNDS = 7,
+    RPP_GB_NOT_IMPLEMENTED = 8,
+    RPP_GB_INTERNAL = 9
+};
+
+enum rpp_gb_dtype { RPP_GB_F32 = 0, RPP_GB_F64 = 1 };
+
+/* rpp::ops::FTInplaceFMAType (include/rpp/operations/basic/ft_inplace_fma.hpp:17-21) */
+enum rpp_gb_inplace_fma_kind {
+    RPP_GB_A_EQUALS_BC_PLUS_A = 0, /* a <- alpha*a + beta*b(x)c */
+    RPP_GB_A_EQUALS_AB_PLUS_C = 1, /* a <- alpha*c + beta*a(x)b */
+    RPP_GB_A_EQUALS_BA_PLUS_C = 2  /* a <- alpha*c + beta*b(x)a */
+};
+
+/* rpp::ops::TensorAntipodeSigningPolicy (include/rpp/operations/basic/
+ * tensor_generalised_antipode.hpp:14) */
+enum rpp_gb_antipode_policy { RPP_GB_NO_SIGNING = 0, RPP_GB_SIGN_BY_DEGREE = 1 };
+
+/* rpp::sparse::MatrixFormat (include/rpp/sparse/matrix.hpp:10-13) */
+enum rpp_gb_matrix_format { RPP_GB_CSR = 0, RPP_GB_CSC = 1 };
+
+typedef void* rpp_gb_stream;
+
+typedef struct rpp_gb_plan rpp_gb_plan;
+typedef struct rpp_gb_matrix rpp_gb_matrix;
+
+typedef struct rpp_gb_tensor_arg {
+    void* data;
+    int64_t stride;
+    int32_t min_degree;
+    int32_t max_degree;
+} rpp_gb_tensor_arg;
+
+/* A graded vector operand of the sparse products, in begin-relative form:
+ * element b's view starts at data + b*stride + begin and holds `size`
+ * coefficients.  For a view over degrees [lo, hi] of a basis with table
+ * degree_begin, begin = degree_begin[lo] and size = degree_begin[hi+1] - begin
+ * (include/rpp/views/dense_graded_vector_view.hpp: begin()/size()). */
+typedef struct rpp_gb_vector_arg {
+    void* data;
+    int64_t stride;
+    int64_t begin;
+    int64_t size;
+} rpp_gb_vector_arg;
+
+/* ------------------------------------------------------------------------
+ * Plans.  A plan fixes (width, depth) and caches the device-side basis
+ * tables the reference re-uploads on every launch (include/rpp/gpu/device.hpp:
+ * 176-209 via include/rpp/basis/tensor_basis.hpp:104-117).  It is immutable
+ * after creation and may be shared by concurrent calls on any streams.
+ * width in [1, 255] (include/rpp/architecture.hpp:36-39), depth in [0, 30].
+ * ---------------------------------------------------------------------- */
+int rpp_gb_plan_create(rpp_gb_plan** plan, int32_t width, int32_t depth, int32_t device);
+int rpp_gb_plan_destroy(rpp_gb_plan* plan);
+const char* rpp_gb_last_error_string(void);
+/* Library version, e.g. "rpp_gb300 1.0.0 sm_103a". */
+const char* rpp_gb_version(void);
+
+/* ------------------------------------------------------------------------
+ * Free-tensor products.
+ * ---------------------------------------------------------------------- */
+
+/* rpp::ops::ft_mul (include/rpp/operations/basic/ft_mul.hpp:48-79):
+ * out = beta * lhs (x) rhs on out's degree range. */
+int rpp_gb_ft_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                  const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* lhs,
+                  const rpp_gb_tensor_arg* rhs, int64_t batch, double beta);
+
+/* rpp::ops::ft_fma (include/rpp/operations/basic/ft_fma.hpp:48-83):
+ * out = alpha*a + beta * b (x) c. */
+int rpp_gb_ft_fma(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                  const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* a,
+                  const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c, int64_t batch,
+                  double alpha, double beta);
+
+/* rpp::ops::ft_inplace_fma<kind> (include/rpp/operations/basic/
+ * ft_inplace_fma.hpp:64-96); `a` is read and written in place. */
+int rpp_gb_ft_inplace_fma(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                          int32_t kind, const rpp_gb_tensor_arg* a, const rpp_gb_tensor_arg* b,
+                          const rpp_gb_tensor_arg* c, int64_t batch, double alpha, double beta);
+
+/* rpp::ops::ft_inplace_mul (include/rpp/operations/basic/ft_inplace_mul.hpp:
+ * 40-69): lhs <- beta * lhs (x) rhs. */
+int rpp_gb_ft_inplace_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                          const rpp_gb_tensor_arg* lhs, const rpp_gb_tensor_arg* rhs,
+                          int64_t batch, double beta);
+
+/* rpp::ops::ft_exp (include/rpp/operations/intermediate/ft_exp.hpp:84-112). */
+int rpp_gb_ft_exp(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                  const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* arg, int64_t batch);
+
+/* rpp::ops::ft_fmexp (include/rpp/operations/intermediate/ft_fmexp.hpp:
+ * 91-121): out = multiplier (x) exp(exponent); out must not alias multiplier. */
+int rpp_gb_ft_fmexp(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                    const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* multiplier,
+                    const rpp_gb_tensor_arg* exponent, int64_t batch);
+
+/* rpp::ops::ft_log (include/rpp/operations/intermediate/ft_log.hpp:87-114). */
+int rpp_gb_ft_log(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                  const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* arg, int64_t batch);
+
+/* rpp::ops::ft_adj_lmul (include/rpp/operations/basic/ft_adj_lmul.hpp:44-73):
+ * out[v] = sum_u op[u] arg[uv]. */
+int rpp_gb_ft_adj_lmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                       const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op,
+                       const rpp_gb_tensor_arg* arg, int64_t batch);
+
+/* rpp::ops::ft_adj_rmul (include/rpp/operations/basic/ft_adj_rmul.hpp:42-71):
+ * out[u] = sum_v op[v] arg[uv]. */
+int rpp_gb_ft_adj_rmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                       const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op,
+                       const rpp_gb_tensor_arg* arg, int64_t batch);
+
+/* rpp::ops::tensor_generalised_antipode<policy> (include/rpp/operations/
+ * basic/tensor_generalised_antipode.hpp:42-69); tensor_antipode and
+ * tensor_reflect are the two policies. */
+int rpp_gb_tensor_antipode(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                           int32_t policy, const rpp_gb_tensor_arg* out,
+                           const rpp_gb_tensor_arg* arg, int64_t batch);
+
+/* Helper ops composed inside the intermediate operations:
+ * rpp::ops::vector_assign (include/rpp/operations/linalg/vector_assign.hpp),
+ * vector_set_constant (vector_set_constant.hpp), tensor_set_identity and
+ * tensor_add_identity (include/rpp/operations/basic/tensor_*_identity.hpp). */
+int rpp_gb_vector_assign(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                         const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* arg,
+                         int64_t batch);
+int rpp_gb_vector_set_constant(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                               const rpp_gb_tensor_arg* out, int64_t batch, double value);
+int rpp_gb_tensor_set_identity(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                               const rpp_gb_tensor_arg* out, int64_t batch, double scalar);
+int rpp_gb_tensor_add_identity(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                               const rpp_gb_tensor_arg* out, int64_t batch, double scalar);
+
+/* ------------------------------------------------------------------------
+ * Sparse matrices and the Lie <-> tensor conversions.
+ * ---------------------------------------------------------------------- */
+
+/* Upload a host compressed matrix once (the reference maps it to the device on
+ * every launch: include/rpp/sparse/detail/compressed_matrix.hpp:157-203).
+ * outer_dim/inner_dim/offsets/indices follow rpp::sparse::CompressedMatrix
+ * (compressed_matrix.hpp:38-125): CSR outer = rows, CSC outer = columns.  A
+ * CSC matrix is transposed to CSR here (the reference's swap_format,
+ * compressed_matrix.hpp:675-744), so products are atomic-free and
+ * deterministic.  Values are stored in both precisions. */
+int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_dim,
+                         int64_t inner_dim, int64_t nnz, const int64_t* offsets,
+                         const int64_t* indices, const double* values, int32_t device);
+int rpp_gb_matrix_destroy(rpp_gb_matrix* matrix);
+
+/* rpp::ops::sparse_matrix_vector_product (include/rpp/operations/linalg/
+ * sparse_matrix_vector.hpp:57-96) with the CPU strategy's begin-relative
+ * indexing (include/rpp/cpu/single_thread/operations/linalg/
+ * sparse_matrix_vector.hpp:57-86, :138-163), batched as one SpMM:
+ * out.begin()[r] = alpha * sum_c M[r][c] arg.begin()[c].  When the matrix was
+ * created from CSC, the whole out view is zeroed first as the CSC product
+ * does; a CSR product writes rows [0, rows) only.  This is also
+ * rpp::ops::tensor_to_lie / lie_to_tensor (include/rpp/operations/basic/
+ * tensor_to_lie.hpp:65-103, lie_to_tensor.hpp:70-108). */
+int rpp_gb_sparse_matrix_vector(const rpp_gb_matrix* matrix, rpp_gb_stream stream,
+                                int32_t dtype, const rpp_gb_vector_arg* out,
+                                const rpp_gb_vector_arg* arg, int64_t batch, double alpha);
+
+/* Hall basis and conversion matrices built natively (restating
+ * include/rpp/basis/hall_basis.hpp:35-88, include/rpp/basis/
+ * lie_multiplication.hpp:163-251, include/rpp/sparse/t2l_matrix.hpp:57-142 and
+ * include/rpp/sparse/l2t_matrix.hpp:58-114, bit-exact).  Query sizes with NULL
+ * outputs first: rpp_gb_lie_basis returns true_size in *true_size and fills
+ * degree_begin (depth+2) and pairs (2*true_size) when non-NULL;
+ * rpp_gb_conversion_matrix fills a CSC matrix (which = 0: tensor_to_lie,
+ * which = 1: lie_to_tensor) when the arrays are non-NULL. */
+int rpp_gb_lie_basis(int32_t width, int32_t depth, int64_t* true_size, int64_t* degree_begin,
+                     int64_t* pairs);
+int rpp_gb_conversion_matrix(int32_t width, int32_t depth, int32_t which, int64_t* outer_dim,
+                             int64_t* inner_dim, int64_t* nnz, int64_t* offsets,
+                             int64_t* indices, double* values);
+
+/* ------------------------------------------------------------------------
+ * Signatures of piecewise-linear paths (no reference counterpart as one
+ * call: the reference caller loops ft_fmexp once per increment,
+ * tests/rpp/gpu/block/ops/ft_fmexp_tests.cu:126-147).
+ *
+ * Increments are a packed ragged array: path b owns increments
+ * [offsets[b], offsets[b+1]) of `incr` (each `width` scalars, row-major).
+ * `offsets` is a DEVICE array of batch+1 int64; pass NULL with `length` > 0
+ * for equal-length paths (offsets[b] = b*length).
+ *
+ * rpp_gb_signature: sig[b] (stride sig_stride) = S(x_b) =
+ *   exp(dx_1) (x) ... (x) exp(dx_L), from the unit tensor.  When seed and
+ * grad are non-NULL the same launch also runs the reverse pass and writes
+ *   grad[k] = d/d(dx_k) sum_b <seed_b, S(x_b)>
+ * (seed b at seed + b*seed_stride), recomputing prefixes backwards by
+ * S_{k-1} = S_k (x) exp(-dx_k) instead of storing them.  sig may be NULL
+ * when only the gradient is wanted.
+ *
+ * rpp_gb_signature_backward: the reverse pass alone, from final signatures
+ * `sig` (as produced by rpp_gb_signature) and cotangents `seed`.
+ * ---------------------------------------------------------------------- */
+int rpp_gb_signature(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                     const void* incr, const int64_t* offsets, int64_t length, int64_t batch,
+                     void* sig, int64_t sig_stride, const void* seed, int64_t seed_stride,
+                     void* grad);
+int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                              const void* incr, const int64_t* offsets, int64_t length,
+                              int64_t batch, const void* sig, int64_t sig_stride,
+                              const void* seed, int64_t seed_stride, void* grad);
+
+/* ------------------------------------------------------------------------
+ * Diagnostics (no reference counterpart).
+ * rpp_gb_fma_peak: measured FMA throughput of `device` in TFLOP/s (2 flops per
+ * FMA) for dtype, from a short dependent-chain kernel; the benchmark uses it
+ * as the roofline denominator of the FMA-bound kernels.  Allocates a small
+ * scratch buffer and synchronises the device.
+ * ---------------------------------------------------------------------- */
+int rpp_gb_fma_peak(int32_t dtype, int32_t device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RPP_GB300_H */

@@ -1,0 +1,639 @@
+// capi.cpp -- the C ABI of include/rpp_gb300.h: plans, matrix handles,
+// argument validation, error mapping and dispatch to the kernel launchers.
+//
+// Error convention: every entry point returns an rpp::ErrorCode value
+// (include/rpp/support/error.hpp:28-39) and records a message readable with
+// rpp_gb_last_error_string() on the same host thread.  CUDA runtime errors
+// are classified like the reference's map_cuda_error
+// (include/rpp/gpu/device.hpp:27-140).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/rpp_gb300.h"
+#include "lie_tables.hpp"
+#include "ops.hpp"
+
+struct rpp_gb_plan {
+    rpp_gb::Geometry geometry;
+    rpp_gb::DeviceInfo device;
+};
+
+struct rpp_gb_matrix {
+    rpp_gb::CsrDevice csr;
+    int32_t device;
+    void* allocation;  // one device block holding offsets, cols and both value arrays
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int ok() {
+    g_last_error.clear();
+    return RPP_GB_SUCCESS;
+}
+
+int map_cuda(cudaError_t err) {
+    switch (err) {
+        case cudaSuccess:
+            return RPP_GB_SUCCESS;
+        case cudaErrorInvalidValue:
+        case cudaErrorInvalidDevice:
+        case cudaErrorInvalidSymbol:
+        case cudaErrorInvalidPitchValue:
+        case cudaErrorInvalidResourceHandle:
+        case cudaErrorInvalidConfiguration:
+        case cudaErrorInvalidClusterSize:
+        case cudaErrorInvalidKernelImage:
+        case cudaErrorInvalidPtx:
+        case cudaErrorInvalidSource:
+        case cudaErrorInvalidDevicePointer:
+            return RPP_GB_INVALID_ARGUMENT;
+        case cudaErrorMemoryAllocation:
+        case cudaErrorLaunchOutOfResources:
+        case cudaErrorOperatingSystem:
+        case cudaErrorInitializationError:
+        case cudaErrorInsufficientDriver:
+        case cudaErrorNoDevice:
+        case cudaErrorDevicesUnavailable:
+            return RPP_GB_OUT_OF_RESOURCES;
+        case cudaErrorLaunchTimeout:
+            return RPP_GB_TIMEOUT;
+        case cudaErrorNotReady:
+            return RPP_GB_CANCELLED;
+        case cudaErrorNotSupported:
+        case cudaErrorUnsupportedLimit:
+        case cudaErrorUnsupportedPtxVersion:
+        case cudaErrorJitCompilerNotFound:
+        case cudaErrorCallRequiresNewerDriver:
+        case cudaErrorStreamCaptureUnsupported:
+        case cudaErrorNoKernelImageForDevice:
+            return RPP_GB_NOT_IMPLEMENTED;
+        case cudaErrorLaunchFailure:
+        case cudaErrorAssert:
+        case cudaErrorIllegalState:
+        case cudaErrorStreamCaptureInvalidated:
+        case cudaErrorStreamCaptureMerge:
+        case cudaErrorStreamCaptureUnmatched:
+        case cudaErrorStreamCaptureUnjoined:
+        case cudaErrorStreamCaptureIsolation:
+        case cudaErrorStreamCaptureImplicit:
+        case cudaErrorCapturedEvent:
+        case cudaErrorStreamCaptureWrongThread:
+        case cudaErrorIllegalAddress:
+        case cudaErrorIllegalInstruction:
+        case cudaErrorMisalignedAddress:
+        case cudaErrorHardwareStackError:
+            return RPP_GB_CONTRACT_VIOLATION;
+        case cudaErrorECCUncorrectable:
+        case cudaErrorSharedObjectSymbolNotFound:
+        case cudaErrorSharedObjectInitFailed:
+        case cudaErrorStartupFailure:
+        case cudaErrorCudartUnloading:
+        case cudaErrorSystemNotReady:
+        case cudaErrorSystemDriverMismatch:
+        case cudaErrorUnknown:
+            return RPP_GB_INTERNAL;
+        default:
+            return RPP_GB_UNKNOWN;
+    }
+}
+
+int cuda_status(cudaError_t err, const char* where) {
+    if (err == cudaSuccess) return ok();
+    return fail(map_cuda(err), std::string(where) + ": " + cudaGetErrorString(err));
+}
+
+// Make the plan's device current for the duration of a call.
+class DeviceGuard {
+public:
+    explicit DeviceGuard(int device) {
+        cudaGetDevice(&prev_);
+        if (prev_ != device) {
+            err_ = cudaSetDevice(device);
+            switched_ = err_ == cudaSuccess;
+        }
+    }
+    ~DeviceGuard() {
+        if (switched_) cudaSetDevice(prev_);
+    }
+    cudaError_t error() const { return err_; }
+
+private:
+    int prev_ = 0;
+    bool switched_ = false;
+    cudaError_t err_ = cudaSuccess;
+};
+
+bool valid_dtype(int32_t dtype) { return dtype == RPP_GB_F32 || dtype == RPP_GB_F64; }
+
+// Normalise a view's degree range to [lo, min(hi, depth)] (empty when lo > hi).
+// Outputs (is_output) must not overlap between batch elements; inputs may
+// use any non-negative stride, including 0 to broadcast one tensor.
+template <typename T>
+bool to_targ(const rpp_gb_tensor_arg* a, const rpp_gb::Geometry& g, bool required, int64_t batch,
+             rpp_gb::TArg<T>& out, const char* name, bool is_output = false) {
+    out = rpp_gb::TArg<T>{nullptr, 0, 1, 0};
+    if (!a) {
+        if (required) {
+            fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + " is NULL");
+            return false;
+        }
+        return true;
+    }
+    if (a->min_degree < 0) {
+        fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + ": negative min_degree");
+        return false;
+    }
+    if (a->stride < 0) {
+        fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + ": negative batch stride");
+        return false;
+    }
+    const int32_t hi = std::min<int32_t>(a->max_degree, g.depth);
+    const bool empty = a->min_degree > hi;
+    if (!a->data && !empty && batch > 0) {
+        fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + ": NULL data for a non-empty view");
+        return false;
+    }
+    if (is_output && !empty && a->stride < static_cast<int64_t>(g.db[hi + 1]) && batch > 1) {
+        fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + ": stride shorter than the view");
+        return false;
+    }
+    out.p = static_cast<T*>(a->data);
+    out.stride = a->stride;
+    out.lo = empty ? 1 : a->min_degree;
+    out.hi = empty ? 0 : hi;
+    return true;
+}
+
+template <typename F>
+int with_plan(const rpp_gb_plan* plan, int32_t dtype, int64_t batch, F&& body) {
+    if (!plan) return fail(RPP_GB_INVALID_ARGUMENT, "plan is NULL");
+    if (!valid_dtype(dtype)) return fail(RPP_GB_INVALID_ARGUMENT, "unknown dtype");
+    if (batch < 0) return fail(RPP_GB_INVALID_ARGUMENT, "negative batch size");
+    if (batch == 0) return ok();
+    DeviceGuard guard(plan->device.device);
+    if (guard.error() != cudaSuccess) return cuda_status(guard.error(), "cudaSetDevice");
+    return body();
+}
+
+template <typename T>
+int run_product(const rpp_gb_plan* plan, cudaStream_t s, rpp_gb::ProductKind kind, const rpp_gb_tensor_arg* out,
+                const rpp_gb_tensor_arg* x, const rpp_gb_tensor_arg* y, const rpp_gb_tensor_arg* z,
+                int64_t batch, double alpha, double beta, bool need_x) {
+    rpp_gb::TArg<T> o, a, b, c;
+    const auto& g = plan->geometry;
+    if (!to_targ(out, g, true, batch, o, "out", true) || !to_targ(x, g, need_x, batch, a, "a") ||
+        !to_targ(y, g, true, batch, b, "b") || !to_targ(z, g, kind != rpp_gb::ProductKind::InplaceMul, batch, c, "c"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    return cuda_status(rpp_gb::launch_product<T>(g, plan->device, s, kind, o, a, b, c, batch, alpha, beta),
+                       "product kernel");
+}
+
+int run_product_any(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, rpp_gb::ProductKind kind,
+                    const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* x, const rpp_gb_tensor_arg* y,
+                    const rpp_gb_tensor_arg* z, int64_t batch, double alpha, double beta, bool need_x) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_product<double>(plan, s, kind, out, x, y, z, batch, alpha, beta, need_x)
+                                   : run_product<float>(plan, s, kind, out, x, y, z, batch, alpha, beta, need_x);
+    });
+}
+
+template <typename T>
+int run_intermediate(const rpp_gb_plan* plan, cudaStream_t s, rpp_gb::IntermediateKind kind,
+                     const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* x, const rpp_gb_tensor_arg* m,
+                     int64_t batch) {
+    rpp_gb::TArg<T> o, a, b;
+    const auto& g = plan->geometry;
+    if (!to_targ(out, g, true, batch, o, "out", true) || !to_targ(x, g, true, batch, a, "arg") ||
+        !to_targ(m, g, kind == rpp_gb::IntermediateKind::FMExp, batch, b, "multiplier"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    if (kind == rpp_gb::IntermediateKind::FMExp && out->data == m->data && batch > 0)
+        return fail(RPP_GB_INVALID_ARGUMENT, "ft_fmexp: out must not alias multiplier");
+    return cuda_status(rpp_gb::launch_intermediate<T>(g, plan->device, s, kind, o, a, b, batch),
+                       "intermediate kernel");
+}
+
+int run_intermediate_any(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                         rpp_gb::IntermediateKind kind, const rpp_gb_tensor_arg* out,
+                         const rpp_gb_tensor_arg* x, const rpp_gb_tensor_arg* m, int64_t batch) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_intermediate<double>(plan, s, kind, out, x, m, batch)
+                                   : run_intermediate<float>(plan, s, kind, out, x, m, batch);
+    });
+}
+
+template <typename T>
+int run_adjoint(const rpp_gb_plan* plan, cudaStream_t s, bool left, const rpp_gb_tensor_arg* out,
+                const rpp_gb_tensor_arg* op, const rpp_gb_tensor_arg* arg, int64_t batch) {
+    rpp_gb::TArg<T> o, p, a;
+    const auto& g = plan->geometry;
+    if (!to_targ(out, g, true, batch, o, "out", true) || !to_targ(op, g, true, batch, p, "op") ||
+        !to_targ(arg, g, true, batch, a, "arg"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    return cuda_status(rpp_gb::launch_adjoint<T>(g, plan->device, s, left, o, p, a, batch), "adjoint kernel");
+}
+
+template <typename T>
+int run_helper(const rpp_gb_plan* plan, cudaStream_t s, rpp_gb::HelperKind kind, const rpp_gb_tensor_arg* out,
+               const rpp_gb_tensor_arg* arg, int64_t batch, double value) {
+    rpp_gb::TArg<T> o, a;
+    const auto& g = plan->geometry;
+    if (!to_targ(out, g, true, batch, o, "out", true) ||
+        !to_targ(arg, g, kind == rpp_gb::HelperKind::Assign, batch, a, "arg"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    return cuda_status(rpp_gb::launch_helper<T>(g, plan->device, s, kind, o, a, batch, value), "helper kernel");
+}
+
+int run_helper_any(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, rpp_gb::HelperKind kind,
+                   const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* arg, int64_t batch, double value) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_helper<double>(plan, s, kind, out, arg, batch, value)
+                                   : run_helper<float>(plan, s, kind, out, arg, batch, value);
+    });
+}
+
+template <typename T>
+int run_signature(const rpp_gb_plan* plan, cudaStream_t s, const void* incr, const int64_t* offsets,
+                  int64_t length, int64_t batch, void* sig, int64_t sig_stride, const void* seed,
+                  int64_t seed_stride, void* grad, bool forward) {
+    const auto& g = plan->geometry;
+    if (!offsets && length < 0) return fail(RPP_GB_INVALID_ARGUMENT, "negative path length");
+    if (!incr && (offsets || length > 0)) return fail(RPP_GB_INVALID_ARGUMENT, "increments are NULL");
+    if (sig && sig_stride < static_cast<int64_t>(g.dim))
+        return fail(RPP_GB_INVALID_ARGUMENT, "signature stride shorter than the tensor dimension");
+    if (seed && seed_stride < static_cast<int64_t>(g.dim))
+        return fail(RPP_GB_INVALID_ARGUMENT, "seed stride shorter than the tensor dimension");
+    if ((seed == nullptr) != (grad == nullptr))
+        return fail(RPP_GB_INVALID_ARGUMENT, "seed and grad must be given together");
+    if (!forward && (!sig || !seed))
+        return fail(RPP_GB_INVALID_ARGUMENT, "backward needs the final signatures and the seeds");
+    if (forward && !sig && !grad) return fail(RPP_GB_INVALID_ARGUMENT, "nothing to compute");
+    if (static_cast<int64_t>(g.depth) * g.width > 256)
+        return fail(RPP_GB_NOT_IMPLEMENTED, "signature kernels need depth*width <= 256");
+    rpp_gb::PathBatch paths{offsets, length, batch};
+    return cuda_status(rpp_gb::launch_signature<T>(g, plan->device, s, static_cast<const T*>(incr), paths,
+                                                   static_cast<T*>(sig), sig_stride, static_cast<const T*>(seed),
+                                                   seed_stride, static_cast<T*>(grad), forward),
+                       "signature kernel");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rpp_gb_last_error_string(void) { return g_last_error.c_str(); }
+
+const char* rpp_gb_version(void) { return "rpp_gb300 1.0.0 sm_103a"; }
+
+int rpp_gb_plan_create(rpp_gb_plan** plan, int32_t width, int32_t depth, int32_t device) {
+    if (!plan) return fail(RPP_GB_INVALID_ARGUMENT, "plan output pointer is NULL");
+    *plan = nullptr;
+    if (width < 1 || width > 255) return fail(RPP_GB_INVALID_ARGUMENT, "width must be in [1, 255]");
+    if (depth < 0 || depth > rpp_gb::kMaxDepth) return fail(RPP_GB_INVALID_ARGUMENT, "depth must be in [0, 30]");
+    rpp_gb::Geometry g{};
+    g.width = width;
+    g.depth = depth;
+    uint64_t db = 0, pw = 1;
+    for (int32_t n = 0; n <= depth; ++n) {
+        g.db[n] = static_cast<uint32_t>(db);
+        g.pw[n] = static_cast<uint32_t>(pw);
+        db += pw;
+        if (db >= (uint64_t{1} << 31)) return fail(RPP_GB_OUT_OF_BOUNDS, "tensor dimension must stay below 2^31");
+        pw *= static_cast<uint64_t>(width);
+    }
+    g.db[depth + 1] = static_cast<uint32_t>(db);
+    g.pw[depth + 1] = 0;
+    g.dim = static_cast<uint32_t>(db);
+    g.divw = rpp_gb::FastDiv(static_cast<uint32_t>(width));
+
+    int count = 0;
+    cudaError_t err = cudaGetDeviceCount(&count);
+    if (err != cudaSuccess) return cuda_status(err, "cudaGetDeviceCount");
+    if (device < 0 || device >= count) return fail(RPP_GB_INVALID_ARGUMENT, "no such CUDA device");
+    rpp_gb::DeviceInfo info{};
+    info.device = device;
+    if ((err = cudaDeviceGetAttribute(&info.sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+        return cuda_status(err, "cudaDeviceGetAttribute");
+    if ((err = cudaDeviceGetAttribute(&info.max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device)) !=
+        cudaSuccess)
+        return cuda_status(err, "cudaDeviceGetAttribute");
+    auto* p = new (std::nothrow) rpp_gb_plan;
+    if (!p) return fail(RPP_GB_OUT_OF_RESOURCES, "out of host memory");
+    p->geometry = g;
+    p->device = info;
+    *plan = p;
+    return ok();
+}
+
+int rpp_gb_plan_destroy(rpp_gb_plan* plan) {
+    delete plan;
+    return ok();
+}
+
+int rpp_gb_ft_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                  const rpp_gb_tensor_arg* lhs, const rpp_gb_tensor_arg* rhs, int64_t batch, double beta) {
+    return run_product_any(plan, stream, dtype, rpp_gb::ProductKind::Fma, out, nullptr, lhs, rhs, batch, 0.0, beta,
+                           false);
+}
+
+int rpp_gb_ft_fma(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                  const rpp_gb_tensor_arg* a, const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c, int64_t batch,
+                  double alpha, double beta) {
+    return run_product_any(plan, stream, dtype, rpp_gb::ProductKind::Fma, out, a, b, c, batch, alpha, beta, true);
+}
+
+int rpp_gb_ft_inplace_fma(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, int32_t kind,
+                          const rpp_gb_tensor_arg* a, const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c,
+                          int64_t batch, double alpha, double beta) {
+    rpp_gb::ProductKind k;
+    switch (kind) {
+        case RPP_GB_A_EQUALS_BC_PLUS_A: k = rpp_gb::ProductKind::InplaceBCA; break;
+        case RPP_GB_A_EQUALS_AB_PLUS_C: k = rpp_gb::ProductKind::InplaceABC; break;
+        case RPP_GB_A_EQUALS_BA_PLUS_C: k = rpp_gb::ProductKind::InplaceBAC; break;
+        default: return fail(RPP_GB_INVALID_ARGUMENT, "unknown in-place FMA kind");
+    }
+    return run_product_any(plan, stream, dtype, k, a, nullptr, b, c, batch, alpha, beta, false);
+}
+
+int rpp_gb_ft_inplace_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                          const rpp_gb_tensor_arg* lhs, const rpp_gb_tensor_arg* rhs, int64_t batch, double beta) {
+    return run_product_any(plan, stream, dtype, rpp_gb::ProductKind::InplaceMul, lhs, nullptr, rhs, nullptr, batch,
+                           0.0, beta, false);
+}
+
+int rpp_gb_ft_exp(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                  const rpp_gb_tensor_arg* arg, int64_t batch) {
+    return run_intermediate_any(plan, stream, dtype, rpp_gb::IntermediateKind::Exp, out, arg, nullptr, batch);
+}
+
+int rpp_gb_ft_fmexp(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                    const rpp_gb_tensor_arg* multiplier, const rpp_gb_tensor_arg* exponent, int64_t batch) {
+    return run_intermediate_any(plan, stream, dtype, rpp_gb::IntermediateKind::FMExp, out, exponent, multiplier,
+                                batch);
+}
+
+int rpp_gb_ft_log(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                  const rpp_gb_tensor_arg* arg, int64_t batch) {
+    return run_intermediate_any(plan, stream, dtype, rpp_gb::IntermediateKind::Log, out, arg, nullptr, batch);
+}
+
+int rpp_gb_ft_adj_lmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                       const rpp_gb_tensor_arg* op, const rpp_gb_tensor_arg* arg, int64_t batch) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_adjoint<double>(plan, s, true, out, op, arg, batch)
+                                   : run_adjoint<float>(plan, s, true, out, op, arg, batch);
+    });
+}
+
+int rpp_gb_ft_adj_rmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                       const rpp_gb_tensor_arg* op, const rpp_gb_tensor_arg* arg, int64_t batch) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_adjoint<double>(plan, s, false, out, op, arg, batch)
+                                   : run_adjoint<float>(plan, s, false, out, op, arg, batch);
+    });
+}
+
+int rpp_gb_tensor_antipode(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, int32_t policy,
+                           const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* arg, int64_t batch) {
+    if (policy != RPP_GB_NO_SIGNING && policy != RPP_GB_SIGN_BY_DEGREE)
+        return fail(RPP_GB_INVALID_ARGUMENT, "unknown antipode signing policy");
+    return with_plan(plan, dtype, batch, [&]() -> int {
+        auto s = static_cast<cudaStream_t>(stream);
+        const auto& g = plan->geometry;
+        const bool sign = policy == RPP_GB_SIGN_BY_DEGREE;
+        if (dtype == RPP_GB_F64) {
+            rpp_gb::TArg<double> o, a;
+            if (!to_targ(out, g, true, batch, o, "out", true) || !to_targ(arg, g, true, batch, a, "arg"))
+                return RPP_GB_INVALID_ARGUMENT;
+            return cuda_status(rpp_gb::launch_antipode<double>(g, plan->device, s, sign, o, a, batch), "antipode");
+        }
+        rpp_gb::TArg<float> o, a;
+        if (!to_targ(out, g, true, batch, o, "out", true) || !to_targ(arg, g, true, batch, a, "arg"))
+            return RPP_GB_INVALID_ARGUMENT;
+        return cuda_status(rpp_gb::launch_antipode<float>(g, plan->device, s, sign, o, a, batch), "antipode");
+    });
+}
+
+int rpp_gb_vector_assign(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                         const rpp_gb_tensor_arg* arg, int64_t batch) {
+    return run_helper_any(plan, stream, dtype, rpp_gb::HelperKind::Assign, out, arg, batch, 0.0);
+}
+
+int rpp_gb_vector_set_constant(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                               const rpp_gb_tensor_arg* out, int64_t batch, double value) {
+    return run_helper_any(plan, stream, dtype, rpp_gb::HelperKind::SetConstant, out, nullptr, batch, value);
+}
+
+int rpp_gb_tensor_set_identity(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                               const rpp_gb_tensor_arg* out, int64_t batch, double scalar) {
+    return run_helper_any(plan, stream, dtype, rpp_gb::HelperKind::SetIdentity, out, nullptr, batch, scalar);
+}
+
+int rpp_gb_tensor_add_identity(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                               const rpp_gb_tensor_arg* out, int64_t batch, double scalar) {
+    return run_helper_any(plan, stream, dtype, rpp_gb::HelperKind::AddIdentity, out, nullptr, batch, scalar);
+}
+
+int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_dim, int64_t inner_dim, int64_t nnz,
+                         const int64_t* offsets, const int64_t* indices, const double* values, int32_t device) {
+    if (!matrix) return fail(RPP_GB_INVALID_ARGUMENT, "matrix output pointer is NULL");
+    *matrix = nullptr;
+    if (format != RPP_GB_CSR && format != RPP_GB_CSC) return fail(RPP_GB_INVALID_ARGUMENT, "unknown matrix format");
+    if (outer_dim < 0 || inner_dim < 0 || nnz < 0) return fail(RPP_GB_INVALID_ARGUMENT, "negative matrix size");
+    if (nnz > std::numeric_limits<int32_t>::max() || outer_dim >= std::numeric_limits<int32_t>::max() ||
+        inner_dim >= std::numeric_limits<int32_t>::max())
+        return fail(RPP_GB_OUT_OF_BOUNDS, "matrix too large for 32-bit indices");
+    if (!offsets || (nnz > 0 && (!indices || !values))) return fail(RPP_GB_INVALID_ARGUMENT, "NULL matrix arrays");
+    if (offsets[0] != 0 || offsets[outer_dim] != nnz)
+        return fail(RPP_GB_INVALID_ARGUMENT, "offsets must start at 0 and end at nnz");
+    for (int64_t o = 0; o < outer_dim; ++o)
+        if (offsets[o + 1] < offsets[o]) return fail(RPP_GB_INVALID_ARGUMENT, "offsets must be non-decreasing");
+    for (int64_t e = 0; e < nnz; ++e)
+        if (indices[e] < 0 || indices[e] >= inner_dim)
+            return fail(RPP_GB_OUT_OF_BOUNDS, "matrix index outside the inner dimension");
+
+    // CSR on the host: rows, row offsets, column indices, values.
+    const int64_t rows = format == RPP_GB_CSR ? outer_dim : inner_dim;
+    const int64_t cols = format == RPP_GB_CSR ? inner_dim : outer_dim;
+    std::vector<int32_t> roff(static_cast<size_t>(rows) + 1, 0), rcol(static_cast<size_t>(nnz));
+    std::vector<double> rval(static_cast<size_t>(nnz));
+    if (format == RPP_GB_CSR) {
+        for (int64_t r = 0; r <= rows; ++r) roff[r] = static_cast<int32_t>(offsets[r]);
+        for (int64_t e = 0; e < nnz; ++e) {
+            rcol[e] = static_cast<int32_t>(indices[e]);
+            rval[e] = values[e];
+        }
+    } else {
+        // Transpose (the reference's swap_format): entries of a row keep
+        // ascending column order.
+        for (int64_t e = 0; e < nnz; ++e) ++roff[static_cast<size_t>(indices[e]) + 1];
+        for (int64_t r = 0; r < rows; ++r) roff[r + 1] += roff[r];
+        std::vector<int32_t> pos(roff.begin(), roff.end() - 1);
+        for (int64_t c = 0; c < cols; ++c)
+            for (int64_t e = offsets[c]; e < offsets[c + 1]; ++e) {
+                const int32_t dst = pos[static_cast<size_t>(indices[e])]++;
+                rcol[dst] = static_cast<int32_t>(c);
+                rval[dst] = values[e];
+            }
+    }
+    std::vector<float> rval32(rval.begin(), rval.end());
+
+    int count = 0;
+    cudaError_t err = cudaGetDeviceCount(&count);
+    if (err != cudaSuccess) return cuda_status(err, "cudaGetDeviceCount");
+    if (device < 0 || device >= count) return fail(RPP_GB_INVALID_ARGUMENT, "no such CUDA device");
+    DeviceGuard guard(device);
+    if (guard.error() != cudaSuccess) return cuda_status(guard.error(), "cudaSetDevice");
+
+    auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
+    const size_t b_off = align(roff.size() * sizeof(int32_t));
+    const size_t b_col = align(std::max<size_t>(1, rcol.size()) * sizeof(int32_t));
+    const size_t b_v64 = align(std::max<size_t>(1, rval.size()) * sizeof(double));
+    const size_t b_v32 = align(std::max<size_t>(1, rval32.size()) * sizeof(float));
+    char* block = nullptr;
+    if ((err = cudaMalloc(&block, b_off + b_col + b_v64 + b_v32)) != cudaSuccess) return cuda_status(err, "cudaMalloc");
+    auto* m = new (std::nothrow) rpp_gb_matrix;
+    if (!m) {
+        cudaFree(block);
+        return fail(RPP_GB_OUT_OF_RESOURCES, "out of host memory");
+    }
+    m->allocation = block;
+    m->device = device;
+    auto* d_off = reinterpret_cast<int32_t*>(block);
+    auto* d_col = reinterpret_cast<int32_t*>(block + b_off);
+    auto* d_v64 = reinterpret_cast<double*>(block + b_off + b_col);
+    auto* d_v32 = reinterpret_cast<float*>(block + b_off + b_col + b_v64);
+    err = cudaMemcpy(d_off, roff.data(), roff.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && nnz > 0) err = cudaMemcpy(d_col, rcol.data(), rcol.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && nnz > 0) err = cudaMemcpy(d_v64, rval.data(), rval.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && nnz > 0) err = cudaMemcpy(d_v32, rval32.data(), rval32.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+        cudaFree(block);
+        delete m;
+        return cuda_status(err, "cudaMemcpy");
+    }
+    m->csr = rpp_gb::CsrDevice{d_off, d_col, d_v64, d_v32, rows, cols, nnz, format == RPP_GB_CSC};
+    *matrix = m;
+    return ok();
+}
+
+int rpp_gb_matrix_destroy(rpp_gb_matrix* matrix) {
+    if (!matrix) return ok();
+    DeviceGuard guard(matrix->device);
+    cudaError_t err = cudaFree(matrix->allocation);
+    delete matrix;
+    return cuda_status(err, "cudaFree");
+}
+
+int rpp_gb_sparse_matrix_vector(const rpp_gb_matrix* matrix, rpp_gb_stream stream, int32_t dtype,
+                                const rpp_gb_vector_arg* out, const rpp_gb_vector_arg* arg, int64_t batch,
+                                double alpha) {
+    if (!matrix || !out || !arg) return fail(RPP_GB_INVALID_ARGUMENT, "NULL matrix or operand");
+    if (!valid_dtype(dtype)) return fail(RPP_GB_INVALID_ARGUMENT, "unknown dtype");
+    if (batch < 0) return fail(RPP_GB_INVALID_ARGUMENT, "negative batch size");
+    if (batch == 0) return ok();
+    const auto& m = matrix->csr;
+    if (out->begin < 0 || arg->begin < 0 || out->size < 0 || arg->size < 0)
+        return fail(RPP_GB_INVALID_ARGUMENT, "negative view offset or size");
+    if (m.rows > out->size) return fail(RPP_GB_OUT_OF_BOUNDS, "matrix has more rows than the output view");
+    if (m.cols_dim > arg->size) return fail(RPP_GB_OUT_OF_BOUNDS, "matrix has more columns than the argument view");
+    if (!out->data || !arg->data) return fail(RPP_GB_INVALID_ARGUMENT, "NULL vector data");
+    if (batch > 1 && (out->stride < out->begin + out->size || arg->stride < arg->begin + arg->size))
+        return fail(RPP_GB_INVALID_ARGUMENT, "vector stride shorter than the view");
+    DeviceGuard guard(matrix->device);
+    if (guard.error() != cudaSuccess) return cuda_status(guard.error(), "cudaSetDevice");
+    rpp_gb::DeviceInfo dev{};
+    dev.device = matrix->device;
+    cudaDeviceGetAttribute(&dev.sm_count, cudaDevAttrMultiProcessorCount, dev.device);
+    cudaDeviceGetAttribute(&dev.max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev.device);
+    auto s = static_cast<cudaStream_t>(stream);
+    cudaError_t err;
+    if (dtype == RPP_GB_F64)
+        err = rpp_gb::launch_spmm<double>(m, dev, s, static_cast<double*>(out->data) + out->begin, out->stride,
+                                          out->size, static_cast<const double*>(arg->data) + arg->begin,
+                                          arg->stride, arg->size, batch, alpha);
+    else
+        err = rpp_gb::launch_spmm<float>(m, dev, s, static_cast<float*>(out->data) + out->begin, out->stride,
+                                         out->size, static_cast<const float*>(arg->data) + arg->begin, arg->stride,
+                                         arg->size, batch, alpha);
+    return cuda_status(err, "spmm kernel");
+}
+
+int rpp_gb_lie_basis(int32_t width, int32_t depth, int64_t* true_size, int64_t* degree_begin, int64_t* pairs) {
+    if (width < 1 || width > 255 || depth < 0 || depth > rpp_gb::kMaxDepth)
+        return fail(RPP_GB_INVALID_ARGUMENT, "width must be in [1, 255] and depth in [0, 30]");
+    try {
+        const auto h = rpp_gb::build_hall_basis(width, depth);
+        if (true_size) *true_size = h.true_size();
+        if (degree_begin) std::copy(h.degree_begin.begin(), h.degree_begin.end(), degree_begin);
+        if (pairs) std::copy(h.pairs.begin(), h.pairs.end(), pairs);
+    } catch (const std::bad_alloc&) {
+        return fail(RPP_GB_OUT_OF_RESOURCES, "out of host memory");
+    }
+    return ok();
+}
+
+int rpp_gb_conversion_matrix(int32_t width, int32_t depth, int32_t which, int64_t* outer_dim, int64_t* inner_dim,
+                             int64_t* nnz, int64_t* offsets, int64_t* indices, double* values) {
+    if (width < 1 || width > 255 || depth < 0 || depth > rpp_gb::kMaxDepth)
+        return fail(RPP_GB_INVALID_ARGUMENT, "width must be in [1, 255] and depth in [0, 30]");
+    if (which != 0 && which != 1) return fail(RPP_GB_INVALID_ARGUMENT, "which must be 0 (t2l) or 1 (l2t)");
+    try {
+        const auto h = rpp_gb::build_hall_basis(width, depth);
+        const auto m = rpp_gb::build_conversion_matrix(h, which);
+        if (outer_dim) *outer_dim = m.outer_dim;
+        if (inner_dim) *inner_dim = m.inner_dim;
+        if (nnz) *nnz = static_cast<int64_t>(m.indices.size());
+        if (offsets) std::copy(m.offsets.begin(), m.offsets.end(), offsets);
+        if (indices) std::copy(m.indices.begin(), m.indices.end(), indices);
+        if (values) std::copy(m.values.begin(), m.values.end(), values);
+    } catch (const std::bad_alloc&) {
+        return fail(RPP_GB_OUT_OF_RESOURCES, "out of host memory");
+    }
+    return ok();
+}
+
+int rpp_gb_signature(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* incr,
+                     const int64_t* offsets, int64_t length, int64_t batch, void* sig, int64_t sig_stride,
+                     const void* seed, int64_t seed_stride, void* grad) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_signature<double>(plan, s, incr, offsets, length, batch, sig, sig_stride,
+                                                           seed, seed_stride, grad, true)
+                                   : run_signature<float>(plan, s, incr, offsets, length, batch, sig, sig_stride,
+                                                          seed, seed_stride, grad, true);
+    });
+}
+
+int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* incr,
+                              const int64_t* offsets, int64_t length, int64_t batch, const void* sig,
+                              int64_t sig_stride, const void* seed, int64_t seed_stride, void* grad) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64
+                   ? run_signature<double>(plan, s, incr, offsets, length, batch, const_cast<void*>(sig), sig_stride,
+                                           seed, seed_stride, grad, false)
+                   : run_signature<float>(plan, s, incr, offsets, length, batch, const_cast<void*>(sig), sig_stride,
+                                          seed, seed_stride, grad, false);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,469 @@
+// ft_ops.cu -- per-operation sm_103a kernels of the batched free-tensor path:
+// products (ft_mul, ft_fma, the in-place FMAs, ft_inplace_mul), the Horner
+// intermediates (ft_exp, ft_fmexp, ft_log), the adjoint multiplies, the
+// generalised antipode and the assign/identity helpers.
+//
+// Shape: one CTA per batch element (grid-stride over the batch).  When the
+// operands fit, their in-range levels are staged in shared memory so every
+// split of the product reads on-chip memory; otherwise the kernels read
+// global memory directly and keep in-place updates correct by writing output
+// degrees from the top down with a CTA barrier per degree (the order the
+// reference's in-place kernels use, include/rpp/gpu/block/operations/basic/
+// ft_inplace_fma.hpp:48-92).
+//
+// Products: out[n][i] = beta * sum_k L[n-k][i / W^k] * R[k][i % W^k] with the
+// split degree k restricted to both operands' degree ranges (zero extension,
+// include/rpp/gpu/block/operations/basic/detail/ft_multiply.hpp:14-64).  The
+// splits are walked with one divide-by-W per step (FastDiv), no per-element
+// degree search.
+#include <cstdio>
+
+#include "common.cuh"
+#include "launch_util.cuh"
+#include "ops.hpp"
+
+namespace rpp_gb {
+namespace {
+
+template <typename T>
+struct Opnd {
+    const T* p;
+    int lo;
+    int hi;
+};
+
+template <typename T>
+__device__ __forceinline__ T split_sum(const Geometry& G, const Opnd<T>& L, const Opnd<T>& R, int n,
+                                       uint32_t i) {
+    const int kmin = imax(imax(R.lo, 0), n - L.hi);
+    const int kmax = imin(imin(R.hi, n), n - L.lo);
+    T acc = T(0);
+    if (kmin > kmax) return acc;
+    uint32_t q = i, r = 0, p = 1;
+    for (int k = 0; k < kmin; ++k) {
+        uint32_t qq, rr;
+        G.divw.divmod(q, qq, rr);
+        r += rr * p;
+        p *= static_cast<uint32_t>(G.width);
+        q = qq;
+    }
+    for (int k = kmin;; ++k) {
+        acc = fma(L.p[G.db[n - k] + q], R.p[G.db[k] + r], acc);
+        if (k == kmax) break;
+        uint32_t qq, rr;
+        G.divw.divmod(q, qq, rr);
+        r += rr * p;
+        p *= static_cast<uint32_t>(G.width);
+        q = qq;
+    }
+    return acc;
+}
+
+// Copy levels [lo, hi] of a tensor into the same positions of a shared buffer.
+template <typename T>
+__device__ __forceinline__ void stage(T* dst, const T* src, int lo, int hi, const Geometry& G) {
+    if (lo > hi) return;
+    const uint32_t b = G.db[lo], e = G.db[hi + 1];
+    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) dst[i] = src[i];
+}
+
+// out[n] = alpha*add[n] + beta * L (x) R at level n, for n in [lo, hi], top
+// degree first; `sync` puts a barrier after each degree (needed when L or R
+// alias the destination in global memory).
+template <typename T>
+__device__ void product_levels(const Geometry& G, T* dst, int lo, int hi, const Opnd<T>& add,
+                               T alpha, const Opnd<T>& L, const Opnd<T>& R, T beta, bool sync) {
+    for (int n = hi; n >= lo; --n) {
+        const uint32_t size = G.pw[n];
+        const uint32_t base = G.db[n];
+        const bool has_add = add.p != nullptr && add.lo <= n && n <= add.hi;
+        for (uint32_t i = threadIdx.x; i < size; i += blockDim.x) {
+            T val = beta * split_sum(G, L, R, n, i);
+            if (has_add) val = fma(alpha, add.p[base + i], val);
+            dst[base + i] = val;
+        }
+        if (sync) __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_product(Geometry G, ProductKind kind, TArg<T> out,
+                                                 TArg<T> x, TArg<T> y, TArg<T> z, int64_t batch,
+                                                 T alpha, T beta, int staged) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    const uint32_t dim = G.dim;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        T* dst = out.at(b);
+        // The three operand slots, in global memory.
+        Opnd<T> add{nullptr, 1, 0}, L{nullptr, 1, 0}, R{nullptr, 1, 0};
+        Opnd<T> self{dst, out.lo, out.hi};
+        switch (kind) {
+            case ProductKind::Fma:
+                if (x.p) add = {x.at(b), x.lo, x.hi};
+                L = {y.at(b), y.lo, y.hi};
+                R = {z.at(b), z.lo, z.hi};
+                break;
+            case ProductKind::InplaceBCA:
+                add = self;
+                L = {y.at(b), y.lo, y.hi};
+                R = {z.at(b), z.lo, z.hi};
+                break;
+            case ProductKind::InplaceABC:
+                add = {z.at(b), z.lo, z.hi};
+                L = self;
+                R = {y.at(b), y.lo, y.hi};
+                break;
+            case ProductKind::InplaceBAC:
+                add = {z.at(b), z.lo, z.hi};
+                L = {y.at(b), y.lo, y.hi};
+                R = self;
+                break;
+            case ProductKind::InplaceMul:
+                L = self;
+                R = {y.at(b), y.lo, y.hi};
+                break;
+        }
+        if (staged) {
+            // Snapshot every operand that is read (old values of an in-place
+            // destination included) so the outputs can be written in any order.
+            T* s_add = sm;
+            T* s_l = sm + dim;
+            T* s_r = sm + 2 * dim;
+            if (add.p) stage(s_add, add.p, add.lo, imin(add.hi, G.depth), G);
+            stage(s_l, L.p, L.lo, imin(L.hi, G.depth), G);
+            stage(s_r, R.p, R.lo, imin(R.hi, G.depth), G);
+            __syncthreads();
+            if (add.p) add.p = s_add;
+            L.p = s_l;
+            R.p = s_r;
+            product_levels(G, dst, out.lo, imin(out.hi, G.depth), add, alpha, L, R, beta, false);
+            __syncthreads();
+        } else {
+            product_levels(G, dst, out.lo, imin(out.hi, G.depth), add, alpha, L, R, beta, true);
+        }
+    }
+}
+
+// One Horner intermediate on work buffer `o` (shared or global), following
+// include/rpp/gpu/block/operations/intermediate/ft_exp.hpp:66-81,
+// ft_fmexp.hpp:61-83 and ft_log.hpp:66-83.  Every in-place product reads only
+// lower degrees of `o` (the exponent/argument is truncated to degree >= 1), so
+// a barrier per degree, top degree first, keeps it exact.
+template <typename T>
+__device__ void intermediate_one(const Geometry& G, IntermediateKind kind, T* o, int olo, int ohi,
+                                 Opnd<T> X, Opnd<T> M) {
+    const int D = G.depth;
+    // initialisation: set_identity / assign / set_constant
+    if (olo <= ohi) {
+        const uint32_t bgn = G.db[olo], end = G.db[ohi + 1];
+        for (uint32_t i = bgn + threadIdx.x; i < end; i += blockDim.x) {
+            T v = T(0);
+            if (kind == IntermediateKind::FMExp) {
+                const uint32_t mb = M.lo <= M.hi ? G.db[M.lo] : 0, me = M.lo <= M.hi ? G.db[M.hi + 1] : 0;
+                if (i >= mb && i < me) v = M.p[i];
+            }
+            o[i] = v;
+        }
+    }
+    __syncthreads();
+    if (kind == IntermediateKind::Exp && threadIdx.x == 0 && olo == 0) o[0] = T(1);
+    __syncthreads();
+    const Opnd<T> none{nullptr, 1, 0};
+    for (int d = D; d > 0; --d) {
+        const int tmax = D - d + 1;
+        const Opnd<T> Xt{X.p, imax(1, X.lo), imin(X.hi, tmax)};
+        const T inv = T(1) / static_cast<T>(d);
+        if (kind == IntermediateKind::Exp) {
+            product_levels(G, o, olo, ohi, none, T(0), Opnd<T>{o, olo, ohi}, Xt, inv, true);
+            if (threadIdx.x == 0 && olo == 0) o[0] += T(1);
+            __syncthreads();
+        } else if (kind == IntermediateKind::FMExp) {
+            product_levels(G, o, olo, ohi, M, T(1), Opnd<T>{o, olo, ohi}, Xt, inv, true);
+        } else {
+            const T val = ((d % 2 == 0) ? T(-1) : T(1)) / static_cast<T>(d);
+            if (threadIdx.x == 0 && olo == 0) o[0] += val;
+            __syncthreads();
+            const int thi = imin(ohi, tmax);
+            product_levels(G, o, olo, thi, none, T(0), Opnd<T>{o, olo, thi}, Xt, T(1), true);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_intermediate(Geometry G, IntermediateKind kind, TArg<T> out,
+                                                      TArg<T> x, TArg<T> m, int64_t batch,
+                                                      int staged) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    const uint32_t dim = G.dim;
+    const int ohi = imin(out.hi, G.depth);
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        Opnd<T> X{x.at(b), imax(1, x.lo), imin(x.hi, G.depth)};
+        Opnd<T> M{nullptr, 1, 0};
+        if (kind == IntermediateKind::FMExp) M = {m.at(b), m.lo, imin(m.hi, G.depth)};
+        T* o = out.at(b);
+        if (staged) {
+            T* s_o = sm;
+            T* s_x = sm + dim;
+            T* s_m = sm + 2 * dim;
+            stage(s_x, X.p, X.lo, X.hi, G);
+            if (M.p) stage(s_m, M.p, M.lo, M.hi, G);
+            __syncthreads();
+            X.p = s_x;
+            if (M.p) M.p = s_m;
+            intermediate_one(G, kind, s_o, out.lo, ohi, X, M);
+            __syncthreads();
+            if (out.lo <= ohi)
+                for (uint32_t i = G.db[out.lo] + threadIdx.x; i < G.db[ohi + 1]; i += blockDim.x) o[i] = s_o[i];
+            __syncthreads();
+        } else {
+            intermediate_one(G, kind, o, out.lo, ohi, X, M);
+            __syncthreads();
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Adjoint multiplies (include/rpp/operations/basic/ft_adj_lmul.hpp,
+// ft_adj_rmul.hpp; semantics as tests/rpp/ft_adjoint_test_helper.hpp:55-87):
+//   left:  out[m][j] = sum_p sum_u op[p][u] arg[m+p][u*W^m + j]
+//   right: out[m][j] = sum_p sum_v op[p][v] arg[m+p][j*W^p + v]
+// Narrow output degrees (fewer coefficients than threads) give each output a
+// warp that splits the sum; wide degrees give each output one thread.
+template <typename T>
+__global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> out, TArg<T> op,
+                                                 TArg<T> arg, int64_t batch, int staged) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    const uint32_t dim = G.dim;
+    const int D = G.depth;
+    const int ohi = imin(out.hi, D), phi = imin(op.hi, D), ahi = imin(arg.hi, D);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        const T* P = op.at(b);
+        const T* A = arg.at(b);
+        T* o = out.at(b);
+        if (staged) {
+            stage(sm, P, op.lo, phi, G);
+            stage(sm + dim, A, arg.lo, ahi, G);
+            __syncthreads();
+            P = sm;
+            A = sm + dim;
+        }
+        for (int m = out.lo; m <= ohi; ++m) {
+            const uint32_t wm = G.pw[m];
+            const int pmin = imax(op.lo, arg.lo - m), pmax = imin(phi, ahi - m);
+            if (wm < blockDim.x) {
+                for (uint32_t j = warp; j < wm; j += nwarps) {
+                    T acc = T(0);
+                    for (int p = pmin; p <= pmax; ++p) {
+                        const uint32_t wp = G.pw[p];
+                        const T* Pp = P + G.db[p];
+                        const T* Ap = A + G.db[m + p];
+                        for (uint32_t u = lane; u < wp; u += 32)
+                            acc = fma(Pp[u], left ? Ap[u * wm + j] : Ap[j * wp + u], acc);
+                    }
+                    acc = warp_sum(acc);
+                    if (lane == 0) o[G.db[m] + j] = acc;
+                }
+            } else {
+                for (uint32_t j = threadIdx.x; j < wm; j += blockDim.x) {
+                    T acc = T(0);
+                    for (int p = pmin; p <= pmax; ++p) {
+                        const uint32_t wp = G.pw[p];
+                        const T* Pp = P + G.db[p];
+                        const T* Ap = A + G.db[m + p];
+                        if (left)
+                            for (uint32_t u = 0; u < wp; ++u) acc = fma(Pp[u], Ap[u * wm + j], acc);
+                        else
+                            for (uint32_t u = 0; u < wp; ++u) acc = fma(Pp[u], Ap[j * wp + u], acc);
+                    }
+                    o[G.db[m] + j] = acc;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ int level_of(const Geometry& G, uint32_t idx) {
+    int n = 0;
+    while (n < G.depth && G.db[n + 1] <= idx) ++n;
+    return n;
+}
+
+// Generalised antipode (include/rpp/gpu/block/operations/basic/
+// tensor_generalised_antipode.hpp:44-75): out[rev w] = sign(|w|) arg[w] on
+// out's degree range; degrees missing from arg are zeroed.
+template <typename T>
+__global__ void k_antipode(Geometry G, int sign, TArg<T> out, TArg<T> arg, int64_t batch) {
+    const int ohi = imin(out.hi, G.depth);
+    if (out.lo > ohi) return;
+    const uint32_t bgn = G.db[out.lo], end = G.db[ohi + 1];
+    for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
+        const T* A = arg.at(b);
+        T* o = out.at(b);
+        for (uint32_t idx = bgn + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
+             idx += gridDim.x * blockDim.x) {
+            const int n = level_of(G, idx);
+            const uint32_t i = idx - G.db[n];
+            if (arg.lo <= n && n <= arg.hi) {
+                uint32_t rev = 0, t = i;
+                for (int d = 0; d < n; ++d) {
+                    uint32_t q, r;
+                    G.divw.divmod(t, q, r);
+                    rev = rev * static_cast<uint32_t>(G.width) + r;
+                    t = q;
+                }
+                const T v = A[idx];
+                o[G.db[n] + rev] = (sign && (n & 1)) ? -v : v;
+            } else {
+                o[idx] = T(0);
+            }
+        }
+    }
+}
+
+// vector_assign / vector_set_constant / tensor_set_identity /
+// tensor_add_identity (include/rpp/gpu/block/operations/linalg/
+// vector_assign.hpp:51-112, vector_set_constant.hpp:42-78,
+// basic/tensor_set_identity.hpp:48-57, basic/tensor_add_identity.hpp:37-45).
+template <typename T>
+__global__ void k_helper(Geometry G, HelperKind kind, TArg<T> out, TArg<T> arg, int64_t batch, T value) {
+    const int ohi = imin(out.hi, G.depth);
+    for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
+        T* o = out.at(b);
+        if (kind == HelperKind::AddIdentity) {
+            if (blockIdx.x == 0 && threadIdx.x == 0 && out.lo == 0) o[0] = o[0] + value;
+            continue;
+        }
+        if (out.lo > ohi) continue;
+        const uint32_t bgn = G.db[out.lo], end = G.db[ohi + 1];
+        uint32_t cb = 0, ce = 0;
+        const T* A = nullptr;
+        if (kind == HelperKind::Assign) {
+            const int lo = imax(out.lo, arg.lo), hi = imin(ohi, imin(arg.hi, G.depth));
+            if (lo <= hi) {
+                cb = G.db[lo];
+                ce = G.db[hi + 1];
+            }
+            A = arg.at(b);
+        }
+        for (uint32_t idx = bgn + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
+             idx += gridDim.x * blockDim.x) {
+            T v = kind == HelperKind::SetConstant ? value : T(0);
+            if (kind == HelperKind::Assign && idx >= cb && idx < ce) v = A[idx];
+            if (kind == HelperKind::SetIdentity && idx == 0) v = value;
+            o[idx] = v;
+        }
+    }
+}
+
+constexpr size_t kStageLimit = 200 * 1024;
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_product(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ProductKind kind,
+                           TArg<T> out, TArg<T> x, TArg<T> y, TArg<T> z, int64_t batch, double alpha,
+                           double beta) {
+    if (batch <= 0) return cudaSuccess;
+    constexpr auto kernel = k_product<T>;
+    cudaError_t err = allow_large_smem<kernel>(dev);
+    if (err != cudaSuccess) return err;
+    const size_t smem_need = 3 * static_cast<size_t>(g.dim) * sizeof(T);
+    const int staged = smem_need <= kStageLimit && smem_need <= static_cast<size_t>(dev.max_smem_optin);
+    const size_t smem = staged ? smem_need : 0;
+    const int threads = threads_for(g.pw[g.depth]);
+    dim3 grid;
+    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+    kernel<<<grid, threads, smem, s>>>(g, kind, out, x, y, z, batch, static_cast<T>(alpha),
+                                       static_cast<T>(beta), staged);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_intermediate(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
+                                IntermediateKind kind, TArg<T> out, TArg<T> x, TArg<T> m,
+                                int64_t batch) {
+    if (batch <= 0) return cudaSuccess;
+    constexpr auto kernel = k_intermediate<T>;
+    cudaError_t err = allow_large_smem<kernel>(dev);
+    if (err != cudaSuccess) return err;
+    const size_t smem_need = (kind == IntermediateKind::FMExp ? 3 : 2) * static_cast<size_t>(g.dim) * sizeof(T);
+    const int staged = smem_need <= kStageLimit && smem_need <= static_cast<size_t>(dev.max_smem_optin);
+    const size_t smem = staged ? smem_need : 0;
+    const int threads = threads_for(g.pw[g.depth]);
+    dim3 grid;
+    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+    kernel<<<grid, threads, smem, s>>>(g, kind, out, x, m, batch, staged);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, bool left,
+                           TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch) {
+    if (batch <= 0) return cudaSuccess;
+    constexpr auto kernel = k_adjoint<T>;
+    cudaError_t err = allow_large_smem<kernel>(dev);
+    if (err != cudaSuccess) return err;
+    const size_t smem_need = 2 * static_cast<size_t>(g.dim) * sizeof(T);
+    const int staged = smem_need <= kStageLimit && smem_need <= static_cast<size_t>(dev.max_smem_optin);
+    const size_t smem = staged ? smem_need : 0;
+    const int threads = threads_for(g.pw[g.depth]);
+    dim3 grid;
+    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+    kernel<<<grid, threads, smem, s>>>(g, left ? 1 : 0, out, op, arg, batch, staged);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_antipode(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, bool sign,
+                            TArg<T> out, TArg<T> arg, int64_t batch) {
+    if (batch <= 0) return cudaSuccess;
+    const int threads = 256;
+    const uint32_t span = g.dim;
+    const unsigned gx = (span + threads - 1) / threads;
+    const unsigned gy = static_cast<unsigned>(std::min<int64_t>(batch, 65535));
+    k_antipode<T><<<dim3(gx, gy), threads, 0, s>>>(g, sign ? 1 : 0, out, arg, batch);
+    (void)dev;
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_helper(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, HelperKind kind,
+                          TArg<T> out, TArg<T> arg, int64_t batch, double value) {
+    if (batch <= 0) return cudaSuccess;
+    const int threads = 256;
+    const unsigned gx = (g.dim + threads - 1) / threads;
+    const unsigned gy = static_cast<unsigned>(std::min<int64_t>(batch, 65535));
+    k_helper<T><<<dim3(gx, gy), threads, 0, s>>>(g, kind, out, arg, batch, static_cast<T>(value));
+    (void)dev;
+    return cudaGetLastError();
+}
+
+#define RPP_GB_INSTANTIATE(T)                                                                      \
+    template cudaError_t launch_product<T>(const Geometry&, const DeviceInfo&, cudaStream_t,       \
+                                           ProductKind, TArg<T>, TArg<T>, TArg<T>, TArg<T>,        \
+                                           int64_t, double, double);                               \
+    template cudaError_t launch_intermediate<T>(const Geometry&, const DeviceInfo&, cudaStream_t,  \
+                                                IntermediateKind, TArg<T>, TArg<T>, TArg<T>,       \
+                                                int64_t);                                          \
+    template cudaError_t launch_adjoint<T>(const Geometry&, const DeviceInfo&, cudaStream_t, bool, \
+                                           TArg<T>, TArg<T>, TArg<T>, int64_t);                    \
+    template cudaError_t launch_antipode<T>(const Geometry&, const DeviceInfo&, cudaStream_t,      \
+                                            bool, TArg<T>, TArg<T>, int64_t);                      \
+    template cudaError_t launch_helper<T>(const Geometry&, const DeviceInfo&, cudaStream_t,        \
+                                          HelperKind, TArg<T>, TArg<T>, int64_t, double);
+
+RPP_GB_INSTANTIATE(float)
+RPP_GB_INSTANTIATE(double)
+
+}  // namespace rpp_gb

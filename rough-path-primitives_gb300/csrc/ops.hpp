@@ -1,0 +1,82 @@
+// ops.hpp -- host-side launchers of the sm_103a kernels (internal; the public
+// surface is the C ABI in include/rpp_gb300.h).  Every launcher enqueues on
+// `stream` and returns the launch's cudaError_t.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace rpp_gb {
+
+enum class ProductKind : int {
+    Fma = 0,         // out = alpha*a + beta*b(x)c   (a may be absent)
+    InplaceBCA = 1,  // a = alpha*a + beta*b(x)c
+    InplaceABC = 2,  // a = alpha*c + beta*a(x)b
+    InplaceBAC = 3,  // a = alpha*c + beta*b(x)a
+    InplaceMul = 4,  // a = beta*a(x)b
+};
+
+enum class IntermediateKind : int { Exp = 0, FMExp = 1, Log = 2 };
+
+enum class HelperKind : int { Assign = 0, SetConstant = 1, SetIdentity = 2, AddIdentity = 3 };
+
+struct DeviceInfo {
+    int device;
+    int sm_count;
+    int max_smem_optin;
+};
+
+template <typename T>
+cudaError_t launch_product(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ProductKind kind,
+                           TArg<T> out, TArg<T> x, TArg<T> y, TArg<T> z, int64_t batch, double alpha,
+                           double beta);
+
+template <typename T>
+cudaError_t launch_intermediate(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
+                                IntermediateKind kind, TArg<T> out, TArg<T> x, TArg<T> y,
+                                int64_t batch);
+
+template <typename T>
+cudaError_t launch_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, bool left,
+                           TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch);
+
+template <typename T>
+cudaError_t launch_antipode(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, bool sign,
+                            TArg<T> out, TArg<T> arg, int64_t batch);
+
+template <typename T>
+cudaError_t launch_helper(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, HelperKind kind,
+                          TArg<T> out, TArg<T> arg, int64_t batch, double value);
+
+// CSR SpMM over a batch of begin-relative vector views.
+struct CsrDevice {
+    const int32_t* offsets;  // rows + 1
+    const int32_t* cols;     // nnz
+    const double* values64;  // nnz
+    const float* values32;   // nnz
+    int64_t rows;
+    int64_t cols_dim;
+    int64_t nnz;
+    bool zero_rest;  // matrix came from CSC: zero the whole out view first
+};
+
+template <typename T>
+cudaError_t launch_spmm(const CsrDevice& m, const DeviceInfo& dev, cudaStream_t s, T* out,
+                        int64_t out_stride, int64_t out_size, const T* arg, int64_t arg_stride,
+                        int64_t arg_size, int64_t batch, double alpha);
+
+// Fused signature kernels.
+struct PathBatch {
+    const int64_t* offsets;  // device, batch + 1 (or nullptr)
+    int64_t length;          // equal length when offsets == nullptr
+    int64_t batch;
+};
+
+template <typename T>
+cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
+                             const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
+                             const T* seed, int64_t seed_stride, T* grad, bool forward);
+
+}  // namespace rpp_gb

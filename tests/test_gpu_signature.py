@@ -1,0 +1,158 @@
+"""Fused signature forward / reverse kernels against the oracle.
+
+The oracle's reverse pass stores every prefix and composes ft_adj_lmul,
+ft_adj_rmul and the derivative of the letter-only exponential; the kernel
+recomputes prefixes backwards instead.  Tolerances: 1e-12 relative (FP64),
+1e-5 (FP32 against the FP64 oracle)."""
+import importlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from _helpers import TOL_F32, TOL_F64, assert_close, rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+pkg = importlib.import_module("rough-path-primitives_gb300")
+
+
+def dev(a, dtype=torch.float64):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device="cuda", dtype=dtype)
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.double().cpu().numpy()
+
+
+def run(W, D, incr, offsets=None, length=None, ell=None, dtype=torch.float64, want_sig=True):
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(dtype)
+    B = len(offsets) - 1 if offsets is not None else incr.shape[0] // length
+    sig = torch.full((B, dim), float("nan"), dtype=dtype, device="cuda") if want_sig else None
+    seed = dev(ell, dtype) if ell is not None else None
+    grad = torch.full(incr.shape, float("nan"), dtype=dtype, device="cuda") if ell is not None else None
+    err = pkg.signature(st, None, dev(incr, dtype), basis, B, length=length,
+                        offsets=None if offsets is None else dev(offsets, torch.int64), out=sig, seed=seed, grad=grad)
+    assert err, err.message
+    return (host(sig) if want_sig else None), (host(grad) if grad is not None else None)
+
+
+def test_golden_signature(golden_dir):
+    z = np.load(os.path.join(golden_dir, "signature_w4d4.npz"))
+    W, D = int(z["width"]), int(z["depth"])
+    L = int(z["offsets"][1])
+    sig, _ = run(W, D, z["incr"], length=L)
+    assert_close(sig, z["sig"], TOL_F64, "signature vs reference")
+    sig32, _ = run(W, D, z["incr"], length=L, dtype=torch.float32)
+    assert_close(sig32, z["sig"], TOL_F32, "fp32 signature vs reference")
+
+
+SHAPES = [(2, 3, 4, 16), (3, 4, 8, 32), (5, 5, 6, 256), (4, 4, 16, 64), (2, 8, 4, 32), (8, 4, 4, 16),
+          (16, 3, 2, 8), (1, 4, 3, 5), (3, 1, 5, 7)]
+
+
+@pytest.mark.parametrize("W,D,B,L", SHAPES)
+def test_forward_and_gradient(orc, W, D, B, L):
+    rng = np.random.default_rng(W * 31 + D)
+    incr = rng.normal(0, 1 / np.sqrt(L), (B * L, W))
+    dim = O.tensor_dim(W, D)
+    ell = rng.uniform(-1, 1, (B, dim))
+    offs = np.arange(B + 1) * L
+    esig, egrad = orc.signature(W, D, incr, offs, ell=ell)
+    sig, grad = run(W, D, incr, length=L, ell=ell)
+    assert_close(sig, esig, TOL_F64, "signature")
+    assert_close(grad, egrad, TOL_F64, "gradient")
+    sig32, grad32 = run(W, D, incr, length=L, ell=ell, dtype=torch.float32)
+    assert_close(sig32, esig, TOL_F32 * 10, "fp32 signature")
+    # gradients sum O(L) terms of size O(1): compare relative to their scale
+    scale = max(1.0, float(np.abs(egrad).max()))
+    assert rel_err(grad32 / scale, egrad / scale) < TOL_F32 * 50
+
+
+def test_ragged_batch_with_empty_and_unit_paths(orc):
+    W, D = 3, 4
+    rng = np.random.default_rng(11)
+    lengths = np.array([5, 0, 1, 17, 2, 0, 33])
+    offs = np.concatenate([[0], np.cumsum(lengths)])
+    incr = rng.normal(0, 0.3, (offs[-1], W))
+    dim = O.tensor_dim(W, D)
+    ell = rng.uniform(-1, 1, (len(lengths), dim))
+    esig, egrad = orc.signature(W, D, incr, offs, ell=ell)
+    sig, grad = run(W, D, incr, offsets=offs, ell=ell)
+    assert_close(sig, esig, TOL_F64, "ragged signature")
+    assert_close(grad, egrad, TOL_F64, "ragged gradient")
+    unit = np.zeros(dim)
+    unit[0] = 1
+    assert np.array_equal(sig[1], unit) and np.array_equal(sig[5], unit)
+
+
+def test_gradient_only_and_backward_entry(orc):
+    W, D, B, L = 4, 4, 5, 24
+    rng = np.random.default_rng(12)
+    incr = rng.normal(0, 0.2, (B * L, W))
+    dim = O.tensor_dim(W, D)
+    ell = rng.uniform(-1, 1, (B, dim))
+    esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
+    _, grad = run(W, D, incr, length=L, ell=ell, want_sig=False)
+    assert_close(grad, egrad, TOL_F64, "gradient without signature output")
+    basis = pkg.TensorBasis(W, D)
+    st = pkg.GB300Strategy(torch.float64)
+    g = torch.zeros(B * L, W, dtype=torch.float64, device="cuda")
+    assert pkg.signature_backward(st, None, dev(incr), basis, B, dev(esig), dev(ell), g, length=L)
+    assert_close(host(g), egrad, TOL_F64, "backward from final signatures")
+
+
+def test_gradient_matches_finite_differences():
+    """Central differences (h = 1e-6) of sum_b <ell_b, S(x_b)> computed on the GPU."""
+    W, D, B, L = 3, 4, 2, 6
+    rng = np.random.default_rng(13)
+    incr = rng.normal(0, 0.4, (B * L, W))
+    dim = O.tensor_dim(W, D)
+    ell = rng.uniform(-1, 1, (B, dim))
+    _, grad = run(W, D, incr, length=L, ell=ell)
+    h = 1e-6
+    fd = np.zeros_like(incr)
+    for i in range(incr.shape[0]):
+        for a in range(W):
+            p, m = incr.copy(), incr.copy()
+            p[i, a] += h
+            m[i, a] -= h
+            sp, _ = run(W, D, p, length=L)
+            sm, _ = run(W, D, m, length=L)
+            fd[i, a] = ((sp - sm) * ell).sum() / (2 * h)
+    assert np.max(np.abs(grad - fd)) < 1e-7
+
+
+def test_chen_identity_full_size():
+    """Size-independent property at the headline shape (W5 D5, 4096 paths of
+    256 steps): S(x) = S(first half) (x) S(second half), via the ft_mul kernel,
+    and the gradient is linear in the seed."""
+    W, D, B, L = 5, 5, 4096, 256
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(torch.float64)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    incr = torch.randn(B * L, W, dtype=torch.float64, device="cuda", generator=g) / np.sqrt(L)
+    full = torch.empty(B, dim, dtype=torch.float64, device="cuda")
+    assert pkg.signature(st, None, incr, basis, B, length=L, out=full)
+    halves = incr.view(B, 2, L // 2, W)
+    first = torch.empty_like(full)
+    second = torch.empty_like(full)
+    assert pkg.signature(st, None, halves[:, 0].contiguous().view(-1, W), basis, B, length=L // 2, out=first)
+    assert pkg.signature(st, None, halves[:, 1].contiguous().view(-1, W), basis, B, length=L // 2, out=second)
+    prod = torch.empty_like(full)
+    mk = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
+    assert pkg.ft_mul(st, None, mk(prod), mk(first), mk(second), basis, B)
+    assert_close(host(prod), host(full), TOL_F64, "Chen identity")
+    ell1 = torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    ell2 = torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    g1, g2, g12 = (torch.empty_like(incr) for _ in range(3))
+    for ell, gg in ((ell1, g1), (ell2, g2), (ell1 + 0.5 * ell2, g12)):
+        assert pkg.signature(st, None, incr, basis, B, length=L, seed=ell, grad=gg)
+    lin = g1 + 0.5 * g2
+    assert_close(host(g12), host(lin), 1e-11, "gradient linearity")
