@@ -130,6 +130,34 @@ def cpu_reference(steps: int, warmup: int, world: int, rank: int):
             "ms_per_step": 1e3 * total / steps}
 
 
+def plain_path(pkg, strat, cfg, basis, incr, ell, batch, grad):
+    """The plain per-operation GPU path over the same workload: L launches of
+    ft_fmexp storing every prefix, then per increment (last first) ft_exp,
+    ft_adj_lmul, ft_adj_rmul and the exp VJP.  Returns the final signatures."""
+    import torch
+
+    W, D, L = WIDTH, DEPTH, LENGTH
+    dim = basis.size()
+    dev = incr.device
+    prefixes = torch.empty(L + 1, batch, dim, dtype=torch.float64, device=dev)
+    G, Gn, H, E = (torch.empty(batch, dim, dtype=torch.float64, device=dev) for _ in range(4))
+    full = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
+    # X_k: increment k of every path viewed as the degree-one part of a tensor
+    xview = lambda k: pkg.make_tensor_batch(incr, L * W, 1, 1, offset=k * W - 1)  # noqa: E731
+    pkg.tensor_set_identity(strat, cfg, full(prefixes[0]), basis, batch).raise_if_failed()
+    for k in range(L):
+        pkg.ft_fmexp(strat, cfg, full(prefixes[k + 1]), full(prefixes[k]), xview(k), basis, batch).raise_if_failed()
+    G.copy_(ell)
+    for k in range(L - 1, -1, -1):
+        pkg.ft_exp(strat, cfg, full(E), xview(k), basis, batch).raise_if_failed()
+        pkg.ft_adj_lmul(strat, cfg, full(H), full(prefixes[k]), full(G), basis, batch).raise_if_failed()
+        pkg.exp_letter_vjp(strat, cfg, H, incr, grad, basis, batch, x_stride=L * W, dx_stride=L * W,
+                           x_offset=k * W, dx_offset=k * W).raise_if_failed()
+        pkg.ft_adj_rmul(strat, cfg, full(Gn), full(E), full(G), basis, batch).raise_if_failed()
+        G, Gn = Gn, G
+    return prefixes[L]
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -154,6 +182,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-operation GPU comparator")
+    ap.add_argument("--batch", type=int, default=BATCH,
+                    help="paths per GPU (default: the headline 4096; smaller only for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -181,16 +212,17 @@ def main():
     rc = lib.rpp_gb_fma_peak(1, local, peak.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     fp64_peak = float(peak[0]) if rc == 0 else None
 
-    incr_h, ell_h = make_inputs(1000 + rank, BATCH)
+    batch = args.batch
+    incr_h, ell_h = make_inputs(1000 + rank, batch)
     incr = torch.from_numpy(incr_h).to(dev)
     ell = torch.from_numpy(ell_h).to(dev)
-    sig = torch.empty(BATCH, dim, dtype=torch.float64, device=dev)
+    sig = torch.empty(batch, dim, dtype=torch.float64, device=dev)
     grad = torch.empty_like(incr)
     stream = torch.cuda.current_stream(dev)
     cfg = pkg.DeviceLaunchConfig(stream)
 
     def step():
-        pkg.signature(strat, cfg, incr, basis, BATCH, length=LENGTH, out=sig, seed=ell, grad=grad).raise_if_failed()
+        pkg.signature(strat, cfg, incr, basis, batch, length=LENGTH, out=sig, seed=ell, grad=grad).raise_if_failed()
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -219,19 +251,19 @@ def main():
         t = torch.tensor([elapsed], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed = float(t.item())
-    value = world * BATCH * args.steps / elapsed
+    value = world * batch * args.steps / elapsed
 
     # end to end through the public API with host buffers
     incr_p = torch.from_numpy(incr_h).pin_memory()
     ell_p = torch.from_numpy(ell_h).pin_memory()
-    sig_p = torch.empty(BATCH, dim, dtype=torch.float64).pin_memory()
+    sig_p = torch.empty(batch, dim, dtype=torch.float64).pin_memory()
     grad_p = torch.empty(incr_h.shape, dtype=torch.float64).pin_memory()
     incr_d, ell_d = torch.empty_like(incr), torch.empty_like(ell)
 
     def e2e_step():
         incr_d.copy_(incr_p, non_blocking=True)
         ell_d.copy_(ell_p, non_blocking=True)
-        pkg.signature(strat, cfg, incr_d, basis, BATCH, length=LENGTH, out=sig, seed=ell_d,
+        pkg.signature(strat, cfg, incr_d, basis, batch, length=LENGTH, out=sig, seed=ell_d,
                       grad=grad).raise_if_failed()
         sig_p.copy_(sig, non_blocking=True)
         grad_p.copy_(grad, non_blocking=True)
@@ -251,7 +283,31 @@ def main():
         t = torch.tensor([e2e_elapsed], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_elapsed = float(t.item())
-    e2e_value = world * BATCH * args.steps / e2e_elapsed
+    e2e_value = world * batch * args.steps / e2e_elapsed
+
+    # the plain per-operation GPU path on the same inputs
+    plain = None
+    if not args.no_plain:
+        plain_grad = torch.empty_like(incr)
+        psig = plain_path(pkg, strat, cfg, basis, incr, ell, batch, plain_grad)  # warm-up
+        torch.cuda.synchronize()
+        p_times = []
+        for _ in range(2):
+            e0.record(stream)
+            psig = plain_path(pkg, strat, cfg, basis, incr, ell, batch, plain_grad)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            p_times.append(e0.elapsed_time(e1) / 1e3)
+        p_s = statistics.mean(p_times)
+        agree = float(torch.max(torch.abs(plain_grad - grad) / torch.clamp(torch.abs(grad), min=1.0)).item())
+        agree_sig = float(torch.max(torch.abs(psig - sig) / torch.clamp(torch.abs(sig), min=1.0)).item())
+        plain = {"value": batch / p_s, "unit": "paths/s", "ms_per_step": 1e3 * p_s,
+                 "launches_per_step": 1 + LENGTH + 4 * LENGTH,
+                 "kernels": "ft_fmexp x L (stored prefixes), then per increment ft_exp, ft_adj_lmul, "
+                            "exp VJP, ft_adj_rmul",
+                 "max_rel_diff_vs_fused": {"sig": agree_sig, "grad": agree}}
+        del plain_grad, psig
+        torch.cuda.empty_cache()
 
     # parity spot check of this run's output against the oracle (3 paths)
     if rank == 0:
@@ -270,18 +326,18 @@ def main():
         return
 
     fma_per_path = 4 * LENGTH * step_fma(WIDTH, DEPTH)
-    flops_per_launch = 2.0 * fma_per_path * BATCH
+    flops_per_launch = 2.0 * fma_per_path * batch
     mean_launch_s = statistics.mean(launch_ms) / 1e3
     achieved = flops_per_launch / mean_launch_s / 1e12
     cpu = None if args.no_cpu_baseline else cpu_reference(2, 1, world, rank)
     h2d = incr_h.nbytes + ell_h.nbytes
-    d2h = BATCH * dim * 8 + incr_h.nbytes
+    d2h = batch * dim * 8 + incr_h.nbytes
     line = {
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "signature_fwd_bwd_w5_d5_l256", "width": WIDTH, "depth": DEPTH,
-                   "batch_per_gpu": BATCH, "length": LENGTH, "increments": "N(0,1/256) iid",
+                   "batch_per_gpu": batch, "length": LENGTH, "increments": "N(0,1/256) iid",
                    "seed_functional": "U[-1,1]", "l2": "inputs+outputs 340 MB > L2 (no flush needed)",
                    "kernel": "fused forward+reverse, one launch per step", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp64_fma", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
@@ -292,6 +348,8 @@ def main():
         "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps,
+        "plain": plain,
+        "fused_over_plain": (value / world) / plain["value"] if plain else None,
         "clocks": clk,
         "parity": {"max_rel_err_sig": s_err, "max_rel_err_grad": g_err, "paths_checked": 3},
     }

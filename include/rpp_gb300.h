@@ -249,6 +249,16 @@ int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int
                               int64_t batch, const void* sig, int64_t sig_stride,
                               const void* seed, int64_t seed_stride, void* grad);
 
+/* Vector-Jacobian product of exp for a degree-one argument (no reference
+ * counterpart; it closes the stored-prefix reverse pass composed from
+ * ft_fmexp, ft_exp, ft_adj_lmul and ft_adj_rmul): for batch element b with
+ * letters x[b*x_stride .. +width) and cotangent H (tensor, stride
+ * cotangent_stride) of E = exp(x), writes dx_a = sum_w H[w] dE[w]/dx_a to
+ * dx[b*dx_stride + a]. */
+int rpp_gb_exp_letter_vjp(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                          const void* cotangent, int64_t cotangent_stride, const void* x,
+                          int64_t x_stride, void* dx, int64_t dx_stride, int64_t batch);
+
 /* ------------------------------------------------------------------------
  * Diagnostics (no reference counterpart).
  * rpp_gb_fma_peak: measured FMA throughput of `device` in TFLOP/s (2 flops per

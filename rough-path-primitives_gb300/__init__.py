@@ -31,7 +31,7 @@ __all__ = [
     "ft_fmexp", "ft_log", "ft_adj_lmul", "ft_adj_rmul", "tensor_antipode", "tensor_reflect",
     "tensor_generalised_antipode", "vector_assign", "vector_set_constant",
     "tensor_set_identity", "tensor_add_identity", "sparse_matrix_vector_product",
-    "tensor_to_lie", "lie_to_tensor", "signature", "signature_backward", "build", "library",
+    "tensor_to_lie", "lie_to_tensor", "signature", "signature_backward", "exp_letter_vjp", "build", "library",
 ]
 
 
@@ -178,18 +178,23 @@ def _i64p(a: np.ndarray):
 @dataclass
 class TensorBatch:
     """Batch of dense tensor views (include/rpp/views/dense_tensor_view.hpp:
-    make_tensor_batch): element b is data[b*stride : ...]."""
+    make_tensor_batch): element b is the tensor whose coefficient 0 sits at
+    element ``offset + b*stride`` of ``data``.  Only coefficients inside the
+    degree range are ever touched, so ``offset`` may point before the buffer
+    (e.g. ``-1`` views a row of increments as the degree-1 part of a tensor)."""
 
     data: object
     stride: int
     min_degree: int
     max_degree: int
+    offset: int = 0
 
     def arg(self) -> _lib.TensorArg:
-        return _lib.TensorArg(self.data.data_ptr(), self.stride, self.min_degree, self.max_degree)
+        ptr = self.data.data_ptr() + self.offset * self.data.element_size()
+        return _lib.TensorArg(ptr, self.stride, self.min_degree, self.max_degree)
 
     def truncate(self, lo: int, hi: int) -> "TensorBatch":
-        return TensorBatch(self.data, self.stride, max(lo, self.min_degree), min(hi, self.max_degree))
+        return TensorBatch(self.data, self.stride, max(lo, self.min_degree), min(hi, self.max_degree), self.offset)
 
 
 @dataclass
@@ -202,8 +207,8 @@ class LieBatch:
     max_degree: int
 
 
-def make_tensor_batch(data, stride: int, min_degree: int, max_degree: int) -> TensorBatch:
-    return TensorBatch(data, int(stride), int(min_degree), int(max_degree))
+def make_tensor_batch(data, stride: int, min_degree: int, max_degree: int, offset: int = 0) -> TensorBatch:
+    return TensorBatch(data, int(stride), int(min_degree), int(max_degree), int(offset))
 
 
 def make_lie_batch(data, stride: int, min_degree: int, max_degree: int) -> LieBatch:
@@ -535,6 +540,20 @@ def signature(strategy, config, increments, basis, num_batches, *, length=None, 
         _ptr(increments), _ptr(offsets), 0 if length is None else int(length), num_batches, _ptr(out),
         dim if out_stride is None else out_stride, _ptr(seed), dim if seed_stride is None else seed_stride,
         _ptr(grad)))
+
+
+def exp_letter_vjp(strategy, config, cotangent, x, dx, basis, num_batches, *, cotangent_stride=None,
+                   x_stride=None, dx_stride=None, x_offset=0, dx_offset=0) -> Error:
+    """dx_a = sum_w H[w] d exp(x)[w] / dx_a for degree-one x (rpp_gb_exp_letter_vjp):
+    the last link of the stored-prefix reverse pass built from the per-op kernels."""
+    _check_batches(strategy, *(TensorBatch(t, 0, 0, 0) for t in (cotangent, x, dx)))
+    lib = _lib.load()
+    es = x.element_size()
+    return _status(lib.rpp_gb_exp_letter_vjp(
+        basis.plan(strategy.device), _cfg(config).handle(strategy.device), strategy.dtype_code(),
+        cotangent.data_ptr(), basis.size() if cotangent_stride is None else cotangent_stride,
+        x.data_ptr() + x_offset * es, basis.width if x_stride is None else x_stride,
+        dx.data_ptr() + dx_offset * es, basis.width if dx_stride is None else dx_stride, num_batches))
 
 
 def signature_backward(strategy, config, increments, basis, num_batches, sig, seed, grad, *, length=None,

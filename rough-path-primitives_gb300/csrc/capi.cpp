@@ -611,6 +611,29 @@ int rpp_gb_conversion_matrix(int32_t width, int32_t depth, int32_t which, int64_
     return ok();
 }
 
+int rpp_gb_exp_letter_vjp(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* cotangent,
+                          int64_t cotangent_stride, const void* x, int64_t x_stride, void* dx, int64_t dx_stride,
+                          int64_t batch) {
+    return with_plan(plan, dtype, batch, [&]() -> int {
+        const auto& g = plan->geometry;
+        if (!cotangent || !x || !dx) return fail(RPP_GB_INVALID_ARGUMENT, "NULL operand");
+        if ((batch > 1 && (cotangent_stride < static_cast<int64_t>(g.dim) || x_stride < g.width ||
+                           dx_stride < g.width)) ||
+            cotangent_stride < 0 || x_stride < 0 || dx_stride < 0)
+            return fail(RPP_GB_INVALID_ARGUMENT, "stride shorter than the operand");
+        auto s = static_cast<cudaStream_t>(stream);
+        cudaError_t err =
+            dtype == RPP_GB_F64
+                ? rpp_gb::launch_exp_letter_vjp<double>(g, plan->device, s, static_cast<const double*>(cotangent),
+                                                        cotangent_stride, static_cast<const double*>(x), x_stride,
+                                                        static_cast<double*>(dx), dx_stride, batch)
+                : rpp_gb::launch_exp_letter_vjp<float>(g, plan->device, s, static_cast<const float*>(cotangent),
+                                                       cotangent_stride, static_cast<const float*>(x), x_stride,
+                                                       static_cast<float*>(dx), dx_stride, batch);
+        return cuda_status(err, "exp vjp kernel");
+    });
+}
+
 int rpp_gb_signature(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* incr,
                      const int64_t* offsets, int64_t length, int64_t batch, void* sig, int64_t sig_stride,
                      const void* seed, int64_t seed_stride, void* grad) {

@@ -366,6 +366,69 @@ __global__ void k_helper(Geometry G, HelperKind kind, TArg<T> out, TArg<T> arg, 
     }
 }
 
+// Vector-Jacobian product of the exponential of a degree-one tensor (the
+// last step of the stored-prefix reverse pass composed from the reference's
+// operations): given x (W letters) and a cotangent H of E = exp(x), writes
+//     dx_a = sum_w H[w] dE[w]/dx_a.
+// E_n = E_{n-1} (x) x / n for a degree-one x, so the reverse of that Horner
+// recursion is, top level first,
+//     Ebar_{n-1}[u] += sum_a Ebar_n[ua] x_a / n,   dx_a += sum_u Ebar_n[ua] E_{n-1}[u] / n,
+// with Ebar = H initially.  One CTA per batch element; E and Ebar in shared
+// memory (2 * dim elements), one partial sum per thread for dx.
+template <typename T>
+__global__ void __launch_bounds__(256) k_exp_letter_vjp(Geometry G, const T* H, int64_t h_stride, const T* x,
+                                                        int64_t x_stride, T* dx, int64_t dx_stride,
+                                                        int64_t batch) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* E = reinterpret_cast<T*>(smem_raw);
+    T* Eb = E + G.dim;
+    T* part = Eb + G.dim;
+    const uint32_t W = static_cast<uint32_t>(G.width);
+    const int D = G.depth;
+    const uint32_t slots = blockDim.x / W;
+    const uint32_t my_a = threadIdx.x % W, my_slot = threadIdx.x / W;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        const T* xb = x + b * x_stride;
+        const T* hb = H + b * h_stride;
+        for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) Eb[i] = hb[i];
+        if (threadIdx.x == 0) E[0] = T(1);
+        __syncthreads();
+        for (int n = 1; n <= D; ++n) {
+            const T inv = T(1) / static_cast<T>(n);
+            for (uint32_t i = threadIdx.x; i < G.pw[n]; i += blockDim.x) {
+                uint32_t q, a;
+                G.divw.divmod(i, q, a);
+                E[G.db[n] + i] = E[G.db[n - 1] + q] * (xb[a] * inv);
+            }
+            __syncthreads();
+        }
+        T acc = T(0);
+        for (int n = D; n >= 1; --n) {
+            const T inv = T(1) / static_cast<T>(n);
+            const uint32_t wp = G.pw[n - 1];
+            const T* En1 = E + G.db[n - 1];
+            const T* Ebn = Eb + G.db[n];
+            T* Ebn1 = Eb + G.db[n - 1];
+            for (uint32_t u = threadIdx.x; u < wp; u += blockDim.x) {
+                T s = T(0);
+                for (uint32_t a = 0; a < W; ++a) s = fma(Ebn[u * W + a], xb[a], s);
+                Ebn1[u] = fma(s, inv, Ebn1[u]);
+            }
+            if (my_slot < slots)
+                for (uint32_t u = my_slot; u < wp; u += slots) acc = fma(Ebn[u * W + my_a], En1[u] * inv, acc);
+            __syncthreads();
+        }
+        part[threadIdx.x] = my_slot < slots ? acc : T(0);
+        __syncthreads();
+        if (threadIdx.x < W) {
+            T v = T(0);
+            for (uint32_t s2 = 0; s2 < slots; ++s2) v += part[s2 * W + threadIdx.x];
+            dx[b * dx_stride + threadIdx.x] = v;
+        }
+        __syncthreads();
+    }
+}
+
 constexpr size_t kStageLimit = 200 * 1024;
 
 }  // namespace
@@ -449,6 +512,24 @@ cudaError_t launch_helper(const Geometry& g, const DeviceInfo& dev, cudaStream_t
     return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_exp_letter_vjp(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const T* H,
+                                  int64_t h_stride, const T* x, int64_t x_stride, T* dx, int64_t dx_stride,
+                                  int64_t batch) {
+    if (batch <= 0) return cudaSuccess;
+    constexpr auto kernel = k_exp_letter_vjp<T>;
+    cudaError_t err = allow_large_smem<kernel>(dev);
+    if (err != cudaSuccess) return err;
+    const int threads = threads_for(g.pw[g.depth]);
+    if (threads < g.width) return cudaErrorInvalidConfiguration;
+    const size_t smem = (2 * static_cast<size_t>(g.dim) + threads) * sizeof(T);
+    if (smem > static_cast<size_t>(dev.max_smem_optin)) return cudaErrorInvalidConfiguration;
+    dim3 grid;
+    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+    kernel<<<grid, threads, smem, s>>>(g, H, h_stride, x, x_stride, dx, dx_stride, batch);
+    return cudaGetLastError();
+}
+
 #define RPP_GB_INSTANTIATE(T)                                                                      \
     template cudaError_t launch_product<T>(const Geometry&, const DeviceInfo&, cudaStream_t,       \
                                            ProductKind, TArg<T>, TArg<T>, TArg<T>, TArg<T>,        \
@@ -461,7 +542,10 @@ cudaError_t launch_helper(const Geometry& g, const DeviceInfo& dev, cudaStream_t
     template cudaError_t launch_antipode<T>(const Geometry&, const DeviceInfo&, cudaStream_t,      \
                                             bool, TArg<T>, TArg<T>, int64_t);                      \
     template cudaError_t launch_helper<T>(const Geometry&, const DeviceInfo&, cudaStream_t,        \
-                                          HelperKind, TArg<T>, TArg<T>, int64_t, double);
+                                          HelperKind, TArg<T>, TArg<T>, int64_t, double);          \
+    template cudaError_t launch_exp_letter_vjp<T>(const Geometry&, const DeviceInfo&, cudaStream_t, \
+                                                  const T*, int64_t, const T*, int64_t, T*, int64_t,  \
+                                                  int64_t);
 
 RPP_GB_INSTANTIATE(float)
 RPP_GB_INSTANTIATE(double)

@@ -50,6 +50,11 @@ template <typename T>
 cudaError_t launch_helper(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, HelperKind kind,
                           TArg<T> out, TArg<T> arg, int64_t batch, double value);
 
+template <typename T>
+cudaError_t launch_exp_letter_vjp(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const T* H,
+                                  int64_t h_stride, const T* x, int64_t x_stride, T* dx, int64_t dx_stride,
+                                  int64_t batch);
+
 // CSR SpMM over a batch of begin-relative vector views.
 struct CsrDevice {
     const int32_t* offsets;  // rows + 1
