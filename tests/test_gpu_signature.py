@@ -156,3 +156,36 @@ def test_chen_identity_full_size():
         assert pkg.signature(st, None, incr, basis, B, length=L, seed=ell, grad=gg)
     lin = g1 + 0.5 * g2
     assert_close(host(g12), host(lin), 1e-11, "gradient linearity")
+
+
+@pytest.mark.parametrize("W,D,B,L", [(3, 4, 4, 8), (5, 5, 3, 12)])
+def test_plain_per_operation_reverse_pass(orc, W, D, B, L):
+    """The stored-prefix reverse pass composed from the per-operation kernels
+    (ft_fmexp with increments viewed as degree-one tensors, ft_exp, ft_adj_lmul,
+    ft_adj_rmul, exp VJP) matches the oracle and the fused kernel."""
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(torch.float64)
+    rng = np.random.default_rng(W + 7 * D)
+    incr_h = rng.normal(0, 1 / np.sqrt(L), (B * L, W))
+    ell_h = rng.uniform(-1, 1, (B, dim))
+    incr, ell = dev(incr_h), dev(ell_h)
+    full = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
+    xview = lambda k: pkg.make_tensor_batch(incr, L * W, 1, 1, offset=k * W - 1)  # noqa: E731
+    prefixes = torch.empty(L + 1, B, dim, dtype=torch.float64, device="cuda")
+    assert pkg.tensor_set_identity(st, None, full(prefixes[0]), basis, B)
+    for k in range(L):
+        assert pkg.ft_fmexp(st, None, full(prefixes[k + 1]), full(prefixes[k]), xview(k), basis, B)
+    G, Gn, H, E = (torch.empty(B, dim, dtype=torch.float64, device="cuda") for _ in range(4))
+    grad = torch.full_like(incr, float("nan"))
+    G.copy_(ell)
+    for k in range(L - 1, -1, -1):
+        assert pkg.ft_exp(st, None, full(E), xview(k), basis, B)
+        assert pkg.ft_adj_lmul(st, None, full(H), full(prefixes[k]), full(G), basis, B)
+        assert pkg.exp_letter_vjp(st, None, H, incr, grad, basis, B, x_stride=L * W, dx_stride=L * W,
+                                  x_offset=k * W, dx_offset=k * W)
+        assert pkg.ft_adj_rmul(st, None, full(Gn), full(E), full(G), basis, B)
+        G, Gn = Gn, G
+    esig, egrad = orc.signature(W, D, incr_h, np.arange(B + 1) * L, ell=ell_h)
+    assert_close(host(prefixes[L]), esig, TOL_F64, "plain forward")
+    assert_close(host(grad), egrad, TOL_F64, "plain reverse")
