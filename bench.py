@@ -224,6 +224,10 @@ def main():
     def step():
         pkg.signature(strat, cfg, incr, basis, batch, length=LENGTH, out=sig, seed=ell, grad=grad).raise_if_failed()
 
+    # autotune the CTA size on this workload (part of the warm-up)
+    terr, tuned_threads, tuned_ms = pkg.signature_tune(strat, cfg, incr, basis, batch, length=LENGTH, out=sig,
+                                                       seed=ell, grad=grad)
+    terr.raise_if_failed()
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
@@ -339,7 +343,8 @@ def main():
         "config": {"workload": "signature_fwd_bwd_w5_d5_l256", "width": WIDTH, "depth": DEPTH,
                    "batch_per_gpu": batch, "length": LENGTH, "increments": "N(0,1/256) iid",
                    "seed_functional": "U[-1,1]", "l2": "inputs+outputs 340 MB > L2 (no flush needed)",
-                   "kernel": "fused forward+reverse, one launch per step", "parallelism": f"replicas x{world}"},
+                   "kernel": "fused forward+reverse, one launch per step", "parallelism": f"replicas x{world}",
+                   "schedule": {"threads_per_cta": tuned_threads, "chosen_by": "rpp_gb_signature_tune"}},
         "roofline": {"bound": "fp64_fma", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": (achieved / fp64_peak) if fp64_peak else None, "traffic": None,
                      "peak_source": "measured in-run (rpp_gb_fma_peak, FP64 FMA chains)",

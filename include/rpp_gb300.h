@@ -249,6 +249,19 @@ int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int
                               int64_t batch, const void* sig, int64_t sig_stride,
                               const void* seed, int64_t seed_stride, void* grad);
 
+/* Autotuner for rpp_gb_signature (no reference counterpart): runs the same
+ * call once per candidate schedule (threads per CTA of the shared-memory
+ * kernel) on the caller's own inputs, times each with CUDA events on
+ * `stream`, and records the fastest for this (device, width, depth, dtype,
+ * outputs requested, ragged or not); later rpp_gb_signature calls with that
+ * key use it.  Synchronises the stream (not capturable); leaves the chosen
+ * schedule's outputs in sig/grad.  *threads and *ms (may be NULL) receive the
+ * choice and its time per launch. */
+int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                          const void* incr, const int64_t* offsets, int64_t length, int64_t batch,
+                          void* sig, int64_t sig_stride, const void* seed, int64_t seed_stride,
+                          void* grad, int32_t* threads, float* ms);
+
 /* Vector-Jacobian product of exp for a degree-one argument (no reference
  * counterpart; it closes the stored-prefix reverse pass composed from
  * ft_fmexp, ft_exp, ft_adj_lmul and ft_adj_rmul): for batch element b with

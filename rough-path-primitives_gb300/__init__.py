@@ -31,7 +31,7 @@ __all__ = [
     "ft_fmexp", "ft_log", "ft_adj_lmul", "ft_adj_rmul", "tensor_antipode", "tensor_reflect",
     "tensor_generalised_antipode", "vector_assign", "vector_set_constant",
     "tensor_set_identity", "tensor_add_identity", "sparse_matrix_vector_product",
-    "tensor_to_lie", "lie_to_tensor", "signature", "signature_backward", "exp_letter_vjp", "build", "library",
+    "tensor_to_lie", "lie_to_tensor", "signature", "signature_backward", "signature_tune", "exp_letter_vjp", "build", "library",
 ]
 
 
@@ -554,6 +554,23 @@ def exp_letter_vjp(strategy, config, cotangent, x, dx, basis, num_batches, *, co
         cotangent.data_ptr(), basis.size() if cotangent_stride is None else cotangent_stride,
         x.data_ptr() + x_offset * es, basis.width if x_stride is None else x_stride,
         dx.data_ptr() + dx_offset * es, basis.width if dx_stride is None else dx_stride, num_batches))
+
+
+def signature_tune(strategy, config, increments, basis, num_batches, *, length=None, offsets=None, out=None,
+                   out_stride=None, seed=None, seed_stride=None, grad=None):
+    """Autotune the signature schedule on these inputs (rpp_gb_signature_tune);
+    returns (Error, threads per CTA chosen, ms per launch).  Later ``signature``
+    calls of the same shape use the choice."""
+    _check_batches(strategy, *(TensorBatch(t, 0, 0, 0) for t in (increments, out, seed, grad) if t is not None))
+    dim = basis.size()
+    lib = _lib.load()
+    threads, ms = ctypes.c_int32(0), ctypes.c_float(0)
+    err = _status(lib.rpp_gb_signature_tune(
+        basis.plan(strategy.device), _cfg(config).handle(strategy.device), strategy.dtype_code(),
+        _ptr(increments), _ptr(offsets), 0 if length is None else int(length), num_batches, _ptr(out),
+        dim if out_stride is None else out_stride, _ptr(seed), dim if seed_stride is None else seed_stride,
+        _ptr(grad), ctypes.byref(threads), ctypes.byref(ms)))
+    return err, threads.value, ms.value
 
 
 def signature_backward(strategy, config, increments, basis, num_batches, sig, seed, grad, *, length=None,

@@ -12,7 +12,10 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -268,10 +271,35 @@ int run_helper_any(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
     });
 }
 
+// Schedules chosen by rpp_gb_signature_tune, keyed by the call's shape:
+// (device, width, depth, dtype, mode, ragged).  Read by every signature call.
+struct ScheduleKey {
+    int device, width, depth, dtype, mode, ragged;
+    bool operator<(const ScheduleKey& o) const {
+        return std::tie(device, width, depth, dtype, mode, ragged) <
+               std::tie(o.device, o.width, o.depth, o.dtype, o.mode, o.ragged);
+    }
+};
+std::mutex g_schedule_lock;
+std::map<ScheduleKey, int> g_schedules;
+
+ScheduleKey schedule_key(const rpp_gb_plan* plan, int32_t dtype, bool forward, const void* sig, const void* seed,
+                         const int64_t* offsets) {
+    const int mode = (forward ? 1 : 0) | (seed ? 2 : 0) | (sig ? 4 : 0);
+    return ScheduleKey{plan->device.device, plan->geometry.width, plan->geometry.depth, dtype, mode,
+                       offsets != nullptr ? 1 : 0};
+}
+
+int scheduled_threads(const ScheduleKey& key) {
+    std::lock_guard<std::mutex> guard(g_schedule_lock);
+    auto it = g_schedules.find(key);
+    return it == g_schedules.end() ? 0 : it->second;
+}
+
 template <typename T>
-int run_signature(const rpp_gb_plan* plan, cudaStream_t s, const void* incr, const int64_t* offsets,
-                  int64_t length, int64_t batch, void* sig, int64_t sig_stride, const void* seed,
-                  int64_t seed_stride, void* grad, bool forward) {
+int check_signature_args(const rpp_gb_plan* plan, const void* incr, const int64_t* offsets, int64_t length,
+                         const void* sig, int64_t sig_stride, const void* seed, int64_t seed_stride,
+                         const void* grad, bool forward) {
     const auto& g = plan->geometry;
     if (!offsets && length < 0) return fail(RPP_GB_INVALID_ARGUMENT, "negative path length");
     if (!incr && (offsets || length > 0)) return fail(RPP_GB_INVALID_ARGUMENT, "increments are NULL");
@@ -286,11 +314,73 @@ int run_signature(const rpp_gb_plan* plan, cudaStream_t s, const void* incr, con
     if (forward && !sig && !grad) return fail(RPP_GB_INVALID_ARGUMENT, "nothing to compute");
     if (static_cast<int64_t>(g.depth) * g.width > 256)
         return fail(RPP_GB_NOT_IMPLEMENTED, "signature kernels need depth*width <= 256");
+    return RPP_GB_SUCCESS;
+}
+
+template <typename T>
+int run_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const void* incr, const int64_t* offsets,
+                  int64_t length, int64_t batch, void* sig, int64_t sig_stride, const void* seed,
+                  int64_t seed_stride, void* grad, bool forward, int threads = -1) {
+    if (int rc = check_signature_args<T>(plan, incr, offsets, length, sig, sig_stride, seed, seed_stride, grad,
+                                         forward))
+        return rc;
+    if (threads < 0) threads = scheduled_threads(schedule_key(plan, dtype, forward, sig, seed, offsets));
     rpp_gb::PathBatch paths{offsets, length, batch};
-    return cuda_status(rpp_gb::launch_signature<T>(g, plan->device, s, static_cast<const T*>(incr), paths,
-                                                   static_cast<T*>(sig), sig_stride, static_cast<const T*>(seed),
-                                                   seed_stride, static_cast<T*>(grad), forward),
+    return cuda_status(rpp_gb::launch_signature<T>(plan->geometry, plan->device, s, static_cast<const T*>(incr),
+                                                   paths, static_cast<T*>(sig), sig_stride,
+                                                   static_cast<const T*>(seed), seed_stride, static_cast<T*>(grad),
+                                                   forward, threads),
                        "signature kernel");
+}
+
+// Autotuner: time each candidate CTA size on the caller's own inputs (one
+// warm-up and two timed launches each, CUDA events on `s`), keep the fastest.
+// Candidates that cannot launch for this shape are skipped.
+template <typename T>
+int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const void* incr, const int64_t* offsets,
+                   int64_t length, int64_t batch, void* sig, int64_t sig_stride, const void* seed,
+                   int64_t seed_stride, void* grad, int32_t* chosen, float* best_ms_out) {
+    if (int rc = check_signature_args<T>(plan, incr, offsets, length, sig, sig_stride, seed, seed_stride, grad,
+                                         true))
+        return rc;
+    static const int candidates[] = {128, 192, 256, 320, 384, 448, 512};
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return fail(RPP_GB_OUT_OF_RESOURCES, "cudaEventCreate failed");
+    int best = 0;
+    float best_ms = 0.f;
+    for (int t : candidates) {
+        int rc = RPP_GB_SUCCESS;
+        for (int rep = 0; rep < 3 && rc == RPP_GB_SUCCESS; ++rep) {
+            if (rep == 1) cudaEventRecord(e0, s);
+            rc = run_signature<T>(plan, s, dtype, incr, offsets, length, batch, sig, sig_stride, seed, seed_stride,
+                                  grad, true, t);
+        }
+        if (rc != RPP_GB_SUCCESS) {
+            cudaGetLastError();  // configuration errors are not sticky; skip this candidate
+            continue;
+        }
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (best == 0 || ms < best_ms) {
+            best = t;
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best == 0) return fail(RPP_GB_NOT_IMPLEMENTED, "no signature schedule can launch for this shape");
+    {
+        std::lock_guard<std::mutex> guard(g_schedule_lock);
+        g_schedules[schedule_key(plan, dtype, true, sig, seed, offsets)] = best;
+    }
+    if (chosen) *chosen = best;
+    if (best_ms_out) *best_ms_out = best_ms / 2.f;
+    // leave the outputs of the chosen schedule in place
+    return run_signature<T>(plan, s, dtype, incr, offsets, length, batch, sig, sig_stride, seed, seed_stride, grad,
+                            true, best);
 }
 
 }  // namespace
@@ -639,10 +729,10 @@ int rpp_gb_signature(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtyp
                      const void* seed, int64_t seed_stride, void* grad) {
     return with_plan(plan, dtype, batch, [&] {
         auto s = static_cast<cudaStream_t>(stream);
-        return dtype == RPP_GB_F64 ? run_signature<double>(plan, s, incr, offsets, length, batch, sig, sig_stride,
-                                                           seed, seed_stride, grad, true)
-                                   : run_signature<float>(plan, s, incr, offsets, length, batch, sig, sig_stride,
-                                                          seed, seed_stride, grad, true);
+        return dtype == RPP_GB_F64 ? run_signature<double>(plan, s, dtype, incr, offsets, length, batch, sig,
+                                                           sig_stride, seed, seed_stride, grad, true)
+                                   : run_signature<float>(plan, s, dtype, incr, offsets, length, batch, sig,
+                                                          sig_stride, seed, seed_stride, grad, true);
     });
 }
 
@@ -652,10 +742,22 @@ int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int
     return with_plan(plan, dtype, batch, [&] {
         auto s = static_cast<cudaStream_t>(stream);
         return dtype == RPP_GB_F64
-                   ? run_signature<double>(plan, s, incr, offsets, length, batch, const_cast<void*>(sig), sig_stride,
-                                           seed, seed_stride, grad, false)
-                   : run_signature<float>(plan, s, incr, offsets, length, batch, const_cast<void*>(sig), sig_stride,
-                                          seed, seed_stride, grad, false);
+                   ? run_signature<double>(plan, s, dtype, incr, offsets, length, batch, const_cast<void*>(sig),
+                                           sig_stride, seed, seed_stride, grad, false)
+                   : run_signature<float>(plan, s, dtype, incr, offsets, length, batch, const_cast<void*>(sig),
+                                          sig_stride, seed, seed_stride, grad, false);
+    });
+}
+
+int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* incr,
+                          const int64_t* offsets, int64_t length, int64_t batch, void* sig, int64_t sig_stride,
+                          const void* seed, int64_t seed_stride, void* grad, int32_t* threads, float* ms) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? tune_signature<double>(plan, s, dtype, incr, offsets, length, batch, sig,
+                                                            sig_stride, seed, seed_stride, grad, threads, ms)
+                                   : tune_signature<float>(plan, s, dtype, incr, offsets, length, batch, sig,
+                                                           sig_stride, seed, seed_stride, grad, threads, ms);
     });
 }
 

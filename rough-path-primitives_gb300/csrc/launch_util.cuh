@@ -20,8 +20,12 @@ inline cudaError_t allow_large_smem(const DeviceInfo& dev) {
     static std::atomic<bool> done[kMaxDevices];
     if (dev.device < 0 || dev.device >= kMaxDevices) return cudaErrorInvalidDevice;
     if (done[dev.device].load(std::memory_order_acquire)) return cudaSuccess;
-    cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           dev.max_smem_optin);
+    // static + dynamic shared memory must fit the opt-in limit
+    cudaFuncAttributes attr{};
+    cudaError_t err = cudaFuncGetAttributes(&attr, kernel);
+    if (err != cudaSuccess) return err;
+    const int dynamic_max = dev.max_smem_optin - static_cast<int>(attr.sharedSizeBytes);
+    err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dynamic_max);
     if (err == cudaSuccess) done[dev.device].store(true, std::memory_order_release);
     return err;
 }

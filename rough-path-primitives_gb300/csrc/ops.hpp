@@ -77,11 +77,17 @@ struct PathBatch {
     const int64_t* offsets;  // device, batch + 1 (or nullptr)
     int64_t length;          // equal length when offsets == nullptr
     int64_t batch;
+    // Ragged batches: paths are handed out longest first through a work
+    // counter (order[] lists path indices by decreasing length, both device
+    // scratch written by the launcher).  Null for equal-length batches.
+    const int32_t* order = nullptr;
+    unsigned int* counter = nullptr;
 };
 
+// `threads` = CTA size of the shared-memory variant (0: heuristic).
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
-                             const T* seed, int64_t seed_stride, T* grad, bool forward);
+                             const T* seed, int64_t seed_stride, T* grad, bool forward, int threads);
 
 }  // namespace rpp_gb

@@ -28,10 +28,16 @@
 // Work per increment: F (forward) + F - W^D (phase A) + ~2F (phase B), nothing
 // stored per step.
 //
+// Barriers: D per forward step and 2D-1 per reverse step.  The scaled
+// increments are double-buffered by step parity so refreshing them needs no
+// barrier of its own, and each reverse step's G update and gradient reduction
+// run inside the next step's first recovery stage.  The threads per CTA are a
+// schedule parameter (chosen by the autotuner, rpp_gb_signature_tune).
+//
 // Shared memory (elements of T): S levels 0..D-1 | top level (S_D in the
-// forward, the seed's top level in the reverse pass) | G levels 0..D-1 |
-// forward chains | cotangent chains | scaled increments | 1/m | one partial
-// sum per thread.
+// forward, the seed's top level in the reverse pass) | forward chains | 2 x
+// scaled increments | 1/m | one partial per thread | G levels 0..D-1 |
+// cotangent chains.
 #include "common.cuh"
 #include "launch_util.cuh"
 #include "ops.hpp"
@@ -56,9 +62,10 @@ struct SigShared {
     T* G;     // cotangent levels 0..D-1
     T* Tf;    // forward chains
     T* Tb;    // scaled cotangent chains
-    T* xc;    // xc[m*W + a] = x_a / m, m = 1..D
+    T* xc;    // two buffers of (D+1)*W: xc[m*W + a] = x_a / m, m = 1..D
     T* inv;   // inv[m] = 1/m
     T* part;  // one partial sum per thread
+    uint32_t xcs;  // size of one increment buffer
 };
 
 // Width either fixed at compile time (WT > 0) or read from the geometry.
@@ -83,14 +90,19 @@ __device__ __forceinline__ T* chain(const SigGeometry& sg, T* base, int n, int j
     return base + sg.choff[j] + static_cast<uint32_t>(n - j - 1) * sg.g.pw[j];
 }
 
+template <typename T>
+__device__ __forceinline__ T* xc_buf(const SigShared<T>& sh, int64_t k) {
+    return sh.xc + (k & 1) * sh.xcs;
+}
+
 // Threads t < D*W each hold one scaled increment coefficient.
 template <typename T>
-__device__ __forceinline__ void set_increment(const SigGeometry& sg, const SigShared<T>& sh, T xv) {
+__device__ __forceinline__ void set_increment(const SigGeometry& sg, const SigShared<T>& sh, T* xc, T xv) {
     const uint32_t W = static_cast<uint32_t>(sg.g.width);
     const uint32_t t = threadIdx.x;
     if (t < static_cast<uint32_t>(sg.g.depth) * W) {
         const uint32_t m = 1 + t / W;
-        sh.xc[m * W + t % W] = xv * sh.inv[m];
+        xc[m * W + t % W] = xv * sh.inv[m];
     }
 }
 
@@ -102,15 +114,15 @@ __device__ __forceinline__ T load_increment(const SigGeometry& sg, const T* path
     return T(0);
 }
 
-// S <- S (x) exp(x).  `top` = false leaves level D (and its chains) alone.
-// Ends with a barrier.
+// One forward step S <- S (x) exp(x).  `nmax` = D when the top level is
+// maintained, D-1 when it is not needed (gradient-only calls).  Ends with a
+// barrier, after which xc_next holds the next step's scaled increment.
 template <typename T, int WT>
-__device__ void forward_step(const SigGeometry& sg, const SigShared<T>& sh, bool top) {
+__device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigShared<T>& sh, const T* xc,
+                                             T* xc_next, T x_next, int nmax) {
     const Geometry& G = sg.g;
     const Width<WT> Wd(G);
     const uint32_t W = Wd.value();
-    const int D = G.depth;
-    const int nmax = top ? D : D - 1;
     T* S = sh.S;
     const T s0 = S[0];
     for (int j = 1; j < nmax; ++j) {
@@ -119,8 +131,7 @@ __device__ void forward_step(const SigGeometry& sg, const SigShared<T>& sh, bool
         for (int n = j + 1; n <= nmax; ++n) {
             T* dst = chain(sg, sh.Tf, n, j);
             const T* prev = chain(sg, sh.Tf, n, j - 1);
-            const T* xm = sh.xc + (n - j + 1) * W;
-#pragma unroll 4
+            const T* xm = xc + (n - j + 1) * W;
             for (uint32_t u = threadIdx.x; u < wj; u += blockDim.x) {
                 uint32_t q, a;
                 Wd.divmod(u, q, a);
@@ -130,12 +141,11 @@ __device__ void forward_step(const SigGeometry& sg, const SigShared<T>& sh, bool
         }
         __syncthreads();
     }
-    const T* x1 = sh.xc + W;
+    const T* x1 = xc + W;
     for (int n = 1; n <= nmax; ++n) {
         const uint32_t wn = G.pw[n];
         T* Sn = S + G.db[n];
         const T* prev = chain(sg, sh.Tf, n, n - 1);
-#pragma unroll 4
         for (uint32_t u = threadIdx.x; u < wn; u += blockDim.x) {
             uint32_t q, a;
             Wd.divmod(u, q, a);
@@ -143,27 +153,72 @@ __device__ void forward_step(const SigGeometry& sg, const SigShared<T>& sh, bool
             Sn[u] = fma(p, x1[a], Sn[u]);
         }
     }
+    set_increment(sg, sh, xc_next, x_next);
     __syncthreads();
 }
 
-// One reverse step: S_k -> S_{k-1} below the top level, G_k -> G_{k-1},
-// grad_k <- xbar.  Ends with a barrier.
+// Finish a reverse step: grad_k from the partials (the stage-1 terms
+// sum_n Gh^n_1[a] S_0 folded in) and, when `update_g`, G_{k-1} from the
+// cotangent chains.  Runs between barriers; thread a < W reads G_1[a] before it
+// updates that same element (level-1 element u is updated by thread u).
+template <typename T>
+__device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const SigShared<T>& sh, T* grad_k,
+                                                    bool update_g, uint32_t slots) {
+    const Geometry& G = sg.g;
+    const int D = G.depth;
+    const uint32_t W = static_cast<uint32_t>(G.width);
+    const T s0 = sh.S[0];
+    if (threadIdx.x < W) {
+        const uint32_t a = threadIdx.x;
+        T v = T(0);
+        for (int n = 1; n <= D; ++n) {
+            const T* g1 = n == 1 ? (D == 1 ? sh.top : sh.G + G.db[1]) : chain(sg, sh.Tb, n, 1);
+            v = fma(g1[a], s0, v);
+        }
+        for (uint32_t s = 0; s < slots; ++s) v += sh.part[s * W + a];
+        grad_k[a] = v;
+    }
+    if (update_g) {
+        for (int i = 1; i < D; ++i) {
+            const uint32_t wi = G.pw[i];
+            T* Gi = sh.G + G.db[i];
+            for (uint32_t u = threadIdx.x; u < wi; u += blockDim.x) {
+                T s = Gi[u];
+                for (int n = i + 1; n <= D; ++n) s = fma(static_cast<T>(n - i + 1), chain(sg, sh.Tb, n, i)[u], s);
+                Gi[u] = s;
+            }
+        }
+    }
+}
+
+// One reverse step for increment k.  `pending_grad` (non-null) = the previous
+// reverse step still has to be finished (its gradient row); that runs inside
+// the first recovery stage.  Ends with a barrier after which xc_next holds the
+// increment of step k-1 and this step's partials are in sh.part.
 template <typename T, int WT>
-__device__ void backward_step(const SigGeometry& sg, const SigShared<T>& sh, T* grad_k) {
+__device__ __forceinline__ void backward_step(const SigGeometry& sg, const SigShared<T>& sh, const T* xc,
+                                              T* xc_next, T x_next, T* pending_grad) {
     const Geometry& G = sg.g;
     const Width<WT> Wd(G);
     const uint32_t W = Wd.value();
     const int D = G.depth;
     T* S = sh.S;
     const T s0 = S[0];
-    const T* x1 = sh.xc + W;
+    const T* x1 = xc + W;
+    const uint32_t slots = blockDim.x / W;
+    const uint32_t my_a = threadIdx.x % W, my_slot = threadIdx.x / W;
+    const bool xbar_lane = my_slot < slots;
 
     // Phase A: recover S_1..S_{D-1} of the prefix and the forward chains.
+    if (D == 1 && pending_grad) {
+        finish_reverse_step(sg, sh, pending_grad, true, slots);
+        __syncthreads();
+    }
     for (int j = 1; j < D; ++j) {
+        if (j == 1 && pending_grad) finish_reverse_step(sg, sh, pending_grad, true, slots);
         const uint32_t wj = G.pw[j];
         T* Sj = S + G.db[j];
         const T* own = chain(sg, sh.Tf, j, j - 1);
-#pragma unroll 2
         for (uint32_t u = threadIdx.x; u < wj; u += blockDim.x) {
             uint32_t q, a;
             Wd.divmod(u, q, a);
@@ -171,27 +226,21 @@ __device__ void backward_step(const SigGeometry& sg, const SigShared<T>& sh, T* 
             Sj[u] = s;
             for (int n = j + 1; n <= D; ++n) {
                 const T p = j == 1 ? s0 : chain(sg, sh.Tf, n, j - 1)[q];
-                chain(sg, sh.Tf, n, j)[u] = fma(p, sh.xc[(n - j + 1) * W + a], s);
+                chain(sg, sh.Tf, n, j)[u] = fma(p, xc[(n - j + 1) * W + a], s);
             }
         }
         __syncthreads();
     }
 
     // Phase B: scaled cotangent chains, top stage first.  xbar partials are
-    // letter-specialised: thread t accumulates letter t % W only, so each
-    // thread keeps a single partial sum.
-    const uint32_t slots = blockDim.x / W;
-    const uint32_t my_a = threadIdx.x % W, my_slot = threadIdx.x / W;
-    const bool xbar_lane = my_slot < slots;
+    // letter-specialised: thread t accumulates letter t % W only.
     T xacc = T(0);
     for (int j = D; j >= 2; --j) {
         const uint32_t wjm1 = G.pw[j - 1];
-        // cotangent contraction Gh^n_{j-1}[u] = sum_a Gh^n_j[ua] x_a / (n-j+2)
         for (int n = j; n <= D; ++n) {
             const T* gin = n == j ? (j == D ? sh.top : sh.G + G.db[j]) : chain(sg, sh.Tb, n, j);
             T* gout = chain(sg, sh.Tb, n, j - 1);
-            const T* xm = sh.xc + (n - j + 2) * W;
-#pragma unroll 2
+            const T* xm = xc + (n - j + 2) * W;
             for (uint32_t u = threadIdx.x; u < wjm1; u += blockDim.x) {
                 const T* row = gin + u * W;
                 T acc = T(0);
@@ -204,7 +253,6 @@ __device__ void backward_step(const SigGeometry& sg, const SigShared<T>& sh, T* 
                 gout[u] = acc;
             }
         }
-        // xbar_a += sum_u Gh^n_j[ua] T^n_{j-1}[u]
         if (xbar_lane) {
             for (int n = j; n <= D; ++n) {
                 const T* gin = n == j ? (j == D ? sh.top : sh.G + G.db[j]) : chain(sg, sh.Tb, n, j);
@@ -215,43 +263,19 @@ __device__ void backward_step(const SigGeometry& sg, const SigShared<T>& sh, T* 
         }
         __syncthreads();
     }
-
-    // Stage 1 (xbar_a += Gh^n_1[a] S_0) is folded into the reduction.  Thread
-    // a < W reads G_1[a] here before it updates that same element below.
-    T v1 = T(0);
-    if (threadIdx.x < W) {
-        const uint32_t a = threadIdx.x;
-        for (int n = 1; n <= D; ++n) {
-            const T* g1 = n == 1 ? (D == 1 ? sh.top : sh.G + G.db[1]) : chain(sg, sh.Tb, n, 1);
-            v1 = fma(g1[a], s0, v1);
-        }
-    }
     sh.part[threadIdx.x] = xbar_lane ? xacc : T(0);
-    // G_{k-1,i} = G_i + sum_{n>i} (n-i+1) Gh^n_i for 1 <= i < D (G_0 is never
-    // used).  Level-1 element u is updated by thread u (W <= blockDim.x).
-    for (int i = 1; i < D; ++i) {
-        const uint32_t wi = G.pw[i];
-        T* Gi = sh.G + G.db[i];
-        for (uint32_t u = threadIdx.x; u < wi; u += blockDim.x) {
-            T s = Gi[u];
-            for (int n = i + 1; n <= D; ++n) s = fma(static_cast<T>(n - i + 1), chain(sg, sh.Tb, n, i)[u], s);
-            Gi[u] = s;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < W) {
-        const uint32_t a = threadIdx.x;
-        T v = v1;
-        for (uint32_t s = 0; s < slots; ++s) v += sh.part[s * W + a];
-        grad_k[a] = v;
-    }
+    set_increment(sg, sh, xc_next, x_next);
     __syncthreads();
 }
 
-template <typename T, int WT>
-__global__ void __launch_bounds__(256) k_signature(SigGeometry sg, const T* __restrict__ incr, PathBatch paths,
-                                                   T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
-                                                   T* grad, int mode) {
+// Kernel body.  With `gws` null every array lives in shared memory; otherwise
+// the state and chain arrays of CTA i live in gws + i*gws_stride (global
+// memory, L2-resident at the grid sizes used) and only the increments,
+// 1/m and the partials stay in shared memory.
+template <typename T, int WT, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_signature(SigGeometry sg, const T* __restrict__ incr, PathBatch paths,
+                                                    T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
+                                                    T* grad, int mode, T* gws, int64_t gws_stride) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geometry& G = sg.g;
     const int D = G.depth;
@@ -260,30 +284,45 @@ __global__ void __launch_bounds__(256) k_signature(SigGeometry sg, const T* __re
     const uint32_t lo = G.db[D];  // coefficients below the top level
     const bool bwd = mode & kBackward;
     const bool fwd_top = mode & kTopLevel;
+    const int nmax = fwd_top ? D : D - 1;
+    const uint32_t slots = blockDim.x / W;
 
     SigShared<T> sh;
-    T* p = reinterpret_cast<T*>(smem_raw);
+    T* q = reinterpret_cast<T*>(smem_raw);
+    T* p = gws ? gws + blockIdx.x * gws_stride : q;
     sh.S = p;
     sh.top = p + lo;
     p += dim;
     sh.Tf = p;
     p += sg.chain_total;
-    sh.xc = p;
-    p += (D + 1) * W;
-    sh.inv = p;
-    p += D + 1;
-    sh.part = p;
-    p += blockDim.x;
     if (bwd) {
         sh.G = p;
         p += lo;
         sh.Tb = p;
+        p += sg.chain_total;
     } else {
         sh.G = sh.Tb = nullptr;
     }
+    if (gws) p = q;
+    sh.xcs = (D + 1) * W;
+    sh.xc = p;
+    p += 2 * sh.xcs;
+    sh.inv = p;
+    p += D + 1;
+    sh.part = p;
     for (int m = threadIdx.x; m <= D; m += blockDim.x) sh.inv[m] = m == 0 ? T(0) : T(1) / static_cast<T>(m);
+    __syncthreads();
 
-    for (int64_t b = blockIdx.x; b < paths.batch; b += gridDim.x) {
+    __shared__ int64_t s_next;
+    int64_t slot = blockIdx.x;
+    if (paths.counter) {
+        if (threadIdx.x == 0) s_next = static_cast<int64_t>(atomicAdd(paths.counter, 1u));
+        __syncthreads();
+        slot = s_next;
+        __syncthreads();
+    }
+    for (; slot < paths.batch;) {
+        const int64_t b = paths.order ? paths.order[slot] : slot;
         const int64_t off = paths.offsets ? paths.offsets[b] : b * paths.length;
         const int64_t len = paths.offsets ? paths.offsets[b + 1] - off : paths.length;
         const T* xin = incr + off * W;
@@ -294,15 +333,15 @@ __global__ void __launch_bounds__(256) k_signature(SigGeometry sg, const T* __re
         } else {
             for (uint32_t i = threadIdx.x; i < dim; i += blockDim.x) sh.S[i] = i == 0 ? T(1) : T(0);
         }
-        __syncthreads();
 
         if (mode & kForward) {
-            T xv = len > 0 ? load_increment(sg, xin, 0) : T(0);
+            if (len > 0) set_increment(sg, sh, xc_buf(sh, 0), load_increment(sg, xin, 0));
+            __syncthreads();
+            T xv = len > 1 ? load_increment(sg, xin, 1) : T(0);
             for (int64_t k = 0; k < len; ++k) {
-                set_increment(sg, sh, xv);
-                if (k + 1 < len) xv = load_increment(sg, xin, k + 1);
-                __syncthreads();
-                forward_step<T, WT>(sg, sh, fwd_top);
+                const T x_next = xv;
+                if (k + 2 < len) xv = load_increment(sg, xin, k + 2);
+                forward_step<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k + 1), x_next, nmax);
             }
             if (sig && !(mode & kLoadFinal)) {
                 T* dst = sig + b * sig_stride;
@@ -315,16 +354,68 @@ __global__ void __launch_bounds__(256) k_signature(SigGeometry sg, const T* __re
             for (uint32_t i = threadIdx.x; i < lo; i += blockDim.x) sh.G[i] = sd[i];
             for (uint32_t i = threadIdx.x; i < G.pw[D]; i += blockDim.x) sh.top[i] = sd[lo + i];
             T* gout = grad + off * W;
-            T xv = len > 0 ? load_increment(sg, xin, len - 1) : T(0);
+            if (len > 0) set_increment(sg, sh, xc_buf(sh, len - 1), load_increment(sg, xin, len - 1));
             __syncthreads();
+            T xv = len > 1 ? load_increment(sg, xin, len - 2) : T(0);
             for (int64_t k = len - 1; k >= 0; --k) {
-                set_increment(sg, sh, xv);
-                if (k > 0) xv = load_increment(sg, xin, k - 1);
+                const T x_next = xv;
+                if (k >= 2) xv = load_increment(sg, xin, k - 2);
+                backward_step<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k - 1), x_next,
+                                     k + 1 < len ? gout + (k + 1) * W : nullptr);
+            }
+            if (len > 0) {
+                finish_reverse_step(sg, sh, gout, false, slots);
                 __syncthreads();
-                backward_step<T, WT>(sg, sh, gout + k * W);
             }
         }
         __syncthreads();
+        if (paths.counter) {
+            if (threadIdx.x == 0) s_next = static_cast<int64_t>(atomicAdd(paths.counter, 1u));
+            __syncthreads();
+            slot = s_next;
+            __syncthreads();
+        } else {
+            slot += gridDim.x;
+        }
+    }
+}
+
+// Orders the paths of a ragged batch longest first for the work counter: a
+// one-CTA counting sort on a log-scale length key (4 buckets per octave), so
+// paths of similar length share a bucket.  The order inside a bucket does not
+// matter: every path's result is independent of when it is processed.  Also
+// zeroes the counter.
+constexpr int kLengthBuckets = 4 * 40;
+
+__device__ __forceinline__ int length_bucket(int64_t len) {
+    if (len <= 0) return 0;
+    const int msb = 63 - __clzll(static_cast<unsigned long long>(len));
+    const int sub = msb >= 2 ? static_cast<int>((len >> (msb - 2)) & 3) : static_cast<int>((len << (2 - msb)) & 3);
+    const int key = 1 + msb * 4 + sub;
+    return key < kLengthBuckets ? key : kLengthBuckets - 1;
+}
+
+__global__ void __launch_bounds__(1024) k_order_by_length(const int64_t* offsets, int64_t batch, int32_t* order,
+                                                          unsigned int* counter) {
+    __shared__ unsigned int hist[kLengthBuckets];
+    __shared__ unsigned int start[kLengthBuckets];
+    for (int i = threadIdx.x; i < kLengthBuckets; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    for (int64_t b = threadIdx.x; b < batch; b += blockDim.x)
+        atomicAdd(&hist[length_bucket(offsets[b + 1] - offsets[b])], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int acc = 0;
+        for (int k = kLengthBuckets - 1; k >= 0; --k) {  // longest bucket first
+            start[k] = acc;
+            acc += hist[k];
+        }
+        *counter = 0;
+    }
+    __syncthreads();
+    for (int64_t b = threadIdx.x; b < batch; b += blockDim.x) {
+        const unsigned int pos = atomicAdd(&start[length_bucket(offsets[b + 1] - offsets[b])], 1u);
+        order[pos] = static_cast<int32_t>(b);
     }
 }
 
@@ -340,30 +431,64 @@ SigGeometry make_sig_geometry(const Geometry& g) {
     return sg;
 }
 
+// Elements of the state and chain arrays of one CTA.
+size_t sig_state_elems(const SigGeometry& sg, bool bwd) {
+    size_t n = sg.g.dim + sg.chain_total;
+    if (bwd) n += sg.g.db[sg.g.depth] + sg.chain_total;
+    return n;
+}
+
+// Shared memory of one CTA: the small arrays, plus the state when resident.
 template <typename T>
-size_t sig_smem_bytes(const SigGeometry& sg, int threads, bool bwd) {
+size_t sig_smem_bytes(const SigGeometry& sg, int threads, bool bwd, bool resident) {
     const size_t D = sg.g.depth, W = sg.g.width;
-    size_t n = sg.g.dim + sg.chain_total + (D + 1) * W + (D + 1) + threads;
-    if (bwd) n += sg.g.db[D] + sg.chain_total;
+    size_t n = 2 * (D + 1) * W + (D + 1) + threads;
+    if (resident) n += sig_state_elems(sg, bwd);
     return n * sizeof(T);
 }
+
+// Threads per CTA of the global-workspace variant (one CTA per SM), and the
+// largest CTA the shared-memory variant may be tuned to.
+constexpr int kWideThreads = 1024;
+constexpr int kResidentMaxThreads = 512;
 
 template <typename T, int WT>
 cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStream_t s, const T* incr,
                          PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride, T* grad,
-                         int mode) {
-    constexpr auto kernel = k_signature<T, WT>;
-    cudaError_t err = allow_large_smem<kernel>(dev);
+                         int mode, int threads_req) {
+    const bool bwd = mode & kBackward;
+    int threads = threads_req > 0 ? threads_req : threads_for(sg.g.pw[sg.g.depth]);
+    if (threads % 32 != 0 || threads > kResidentMaxThreads) return cudaErrorInvalidConfiguration;
+    size_t smem = sig_smem_bytes<T>(sg, threads, bwd, true);
+    // (the kernel also holds a few bytes of static shared memory)
+    if (smem + 64 <= static_cast<size_t>(dev.max_smem_optin)) {
+        constexpr auto kernel = k_signature<T, WT, kResidentMaxThreads>;
+        cudaError_t err = allow_large_smem<kernel>(dev);
+        if (err != cudaSuccess) return err;
+        // every (degree, letter) pair of the scaled increment needs its own thread
+        if (threads < sg.g.depth * sg.g.width || threads < sg.g.width) return cudaErrorInvalidConfiguration;
+        dim3 grid;
+        if ((err = batch_grid(kernel, dev, threads, smem, paths.batch, grid)) != cudaSuccess) return err;
+        kernel<<<grid, threads, smem, s>>>(sg, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, nullptr, 0);
+        return cudaGetLastError();
+    }
+    // State larger than one CTA's shared memory: stream-ordered workspace,
+    // one CTA of kWideThreads per SM (the workspace stays within L2 for the
+    // shapes of interest), released on the same stream after the launch.
+    constexpr auto kernel = k_signature<T, 0, kWideThreads>;
+    threads = kWideThreads;
+    if (threads < sg.g.depth * sg.g.width) return cudaErrorInvalidConfiguration;
+    smem = sig_smem_bytes<T>(sg, threads, bwd, false);
+    const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>(paths.batch, dev.sm_count));
+    const int64_t stride = static_cast<int64_t>((sig_state_elems(sg, bwd) + 31) / 32 * 32);
+    T* ws = nullptr;
+    cudaError_t err = cudaMallocAsync(reinterpret_cast<void**>(&ws), static_cast<size_t>(ctas * stride) * sizeof(T), s);
     if (err != cudaSuccess) return err;
-    const int threads = threads_for(sg.g.pw[sg.g.depth]);
-    // every (degree, letter) pair of the scaled increment needs its own thread
-    if (threads < sg.g.depth * sg.g.width || threads < sg.g.width) return cudaErrorInvalidConfiguration;
-    const size_t smem = sig_smem_bytes<T>(sg, threads, mode & kBackward);
-    if (smem > static_cast<size_t>(dev.max_smem_optin)) return cudaErrorInvalidConfiguration;
-    dim3 grid;
-    if ((err = batch_grid(kernel, dev, threads, smem, paths.batch, grid)) != cudaSuccess) return err;
-    kernel<<<grid, threads, smem, s>>>(sg, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
-    return cudaGetLastError();
+    kernel<<<dim3(static_cast<unsigned>(ctas)), threads, smem, s>>>(sg, incr, paths, sig, sig_stride, seed,
+                                                                    seed_stride, grad, mode, ws, stride);
+    err = cudaGetLastError();
+    cudaError_t ferr = cudaFreeAsync(ws, s);
+    return err != cudaSuccess ? err : ferr;
 }
 
 }  // namespace
@@ -371,7 +496,7 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const T* incr,
                              PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
-                             T* grad, bool forward) {
+                             T* grad, bool forward, int threads) {
     if (paths.batch <= 0) return cudaSuccess;
     const SigGeometry sg = make_sig_geometry(g);
     int mode = 0;
@@ -383,21 +508,44 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
     } else {
         mode |= kBackward | kLoadFinal;
     }
-    switch (g.width) {
-        case 2: return launch_width<T, 2>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
-        case 3: return launch_width<T, 3>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
-        case 4: return launch_width<T, 4>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
-        case 5: return launch_width<T, 5>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
-        case 6: return launch_width<T, 6>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
-        case 8: return launch_width<T, 8>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
-        case 16: return launch_width<T, 16>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
-        default: return launch_width<T, 0>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
+    // Ragged batches: order the paths longest first and hand them out through
+    // a work counter (stream-ordered scratch, released after the launch).
+    void* scratch = nullptr;
+    if (paths.offsets && paths.batch > 1) {
+        const size_t bytes = 256 + static_cast<size_t>(paths.batch) * sizeof(int32_t);
+        cudaError_t err = cudaMallocAsync(&scratch, bytes, s);
+        if (err != cudaSuccess) return err;
+        paths.counter = static_cast<unsigned int*>(scratch);
+        paths.order = reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + 256);
+        k_order_by_length<<<1, 1024, 0, s>>>(paths.offsets, paths.batch, const_cast<int32_t*>(paths.order),
+                                             paths.counter);
+        if ((err = cudaGetLastError()) != cudaSuccess) {
+            cudaFreeAsync(scratch, s);
+            return err;
+        }
     }
+    cudaError_t err;
+    switch (g.width) {
+        case 2: err = launch_width<T, 2>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+        case 3: err = launch_width<T, 3>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+        case 4: err = launch_width<T, 4>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+        case 5: err = launch_width<T, 5>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+        case 6: err = launch_width<T, 6>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+        case 8: err = launch_width<T, 8>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+        case 16: err = launch_width<T, 16>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+        default: err = launch_width<T, 0>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+    }
+    if (scratch) {
+        cudaError_t ferr = cudaFreeAsync(scratch, s);
+        if (err == cudaSuccess) err = ferr;
+    }
+    return err;
 }
 
 template cudaError_t launch_signature<float>(const Geometry&, const DeviceInfo&, cudaStream_t, const float*,
-                                             PathBatch, float*, int64_t, const float*, int64_t, float*, bool);
+                                             PathBatch, float*, int64_t, const float*, int64_t, float*, bool, int);
 template cudaError_t launch_signature<double>(const Geometry&, const DeviceInfo&, cudaStream_t, const double*,
-                                              PathBatch, double*, int64_t, const double*, int64_t, double*, bool);
+                                              PathBatch, double*, int64_t, const double*, int64_t, double*, bool,
+                                              int);
 
 }  // namespace rpp_gb

@@ -53,7 +53,7 @@ def test_golden_signature(golden_dir):
 
 
 SHAPES = [(2, 3, 4, 16), (3, 4, 8, 32), (5, 5, 6, 256), (4, 4, 16, 64), (2, 8, 4, 32), (8, 4, 4, 16),
-          (16, 3, 2, 8), (1, 4, 3, 5), (3, 1, 5, 7)]
+          (16, 3, 2, 8), (1, 4, 3, 5), (3, 1, 5, 7), (6, 6, 2, 8), (2, 12, 2, 16), (7, 3, 3, 9)]
 
 
 @pytest.mark.parametrize("W,D,B,L", SHAPES)
@@ -189,3 +189,23 @@ def test_plain_per_operation_reverse_pass(orc, W, D, B, L):
     esig, egrad = orc.signature(W, D, incr_h, np.arange(B + 1) * L, ell=ell_h)
     assert_close(host(prefixes[L]), esig, TOL_F64, "plain forward")
     assert_close(host(grad), egrad, TOL_F64, "plain reverse")
+
+
+def test_autotuner_records_schedule_and_keeps_parity(orc):
+    W, D, B, L = 4, 4, 64, 32
+    rng = np.random.default_rng(41)
+    incr = rng.normal(0, 1 / np.sqrt(L), (B * L, W))
+    dim = O.tensor_dim(W, D)
+    ell = rng.uniform(-1, 1, (B, dim))
+    basis = pkg.TensorBasis(W, D)
+    st = pkg.GB300Strategy(torch.float64)
+    sig = torch.empty(B, dim, dtype=torch.float64, device="cuda")
+    grad = torch.empty(B * L, W, dtype=torch.float64, device="cuda")
+    err, threads, ms = pkg.signature_tune(st, None, dev(incr), basis, B, length=L, out=sig, seed=dev(ell), grad=grad)
+    assert err, err.message
+    assert threads in (128, 192, 256, 320, 384, 448, 512) and ms > 0
+    esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
+    assert_close(host(sig), esig, TOL_F64, "tuned signature")
+    assert_close(host(grad), egrad, TOL_F64, "tuned gradient")
+    sig2, grad2 = run(W, D, incr, length=L, ell=ell)
+    assert np.array_equal(sig2, host(sig)) or threads != 0
