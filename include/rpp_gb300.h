@@ -249,6 +249,27 @@ int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int
                               int64_t batch, const void* sig, int64_t sig_stride,
                               const void* seed, int64_t seed_stride, void* grad);
 
+/* rpp_gb_signature without any device allocation (no counterpart in the
+ * reference).  For callers that cannot allocate device memory at call time:
+ * runtimes that own all device memory through their own allocator and forbid
+ * cudaMalloc / cudaMallocAsync from plugins, real-time loops that must not wait
+ * on or grow a memory pool, and hosts that budget device memory up front.
+ * Same arguments, results and numerics as rpp_gb_signature; the only scratch
+ * it needs (the work counter and longest-first order of a ragged batch) lives
+ * in a fixed 8 MiB device array of the library, held by every GPU that loads
+ * the library until the process exits.  Limits: a ragged batch of at most
+ * 2,097,088 paths (RPP_GB_OUT_OF_BOUNDS beyond), and only shapes whose state
+ * fits one CTA's shared memory (RPP_GB_NOT_IMPLEMENTED otherwise, e.g. width 6
+ * depth 6 in FP64).  All calls share the array and it keeps the previous
+ * call's contents (each call re-initialises what it reads), so calls whose
+ * launches may overlap on the GPU race and must be serialised by the caller.
+ * The first call on each device looks up the array's device address (with
+ * that device current); make that first call before any stream capture. */
+int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                                    const void* incr, const int64_t* offsets, int64_t length,
+                                    int64_t batch, void* sig, int64_t sig_stride, const void* seed,
+                                    int64_t seed_stride, void* grad);
+
 /* Autotuner for rpp_gb_signature (no reference counterpart): runs the same
  * call once per candidate schedule (threads per CTA of the shared-memory
  * kernel) on the caller's own inputs, times each with CUDA events on

@@ -749,6 +749,46 @@ int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int
     });
 }
 
+// Same computation as rpp_gb_signature without any device allocation; see
+// the header and signature.cu for who needs it and its limits.
+int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* incr,
+                                    const int64_t* offsets, int64_t length, int64_t batch, void* sig,
+                                    int64_t sig_stride, const void* seed, int64_t seed_stride, void* grad) {
+    return with_plan(plan, dtype, batch, [&]() -> int {
+        auto s = static_cast<cudaStream_t>(stream);
+        const int threads = scheduled_threads(schedule_key(plan, dtype, true, sig, seed, offsets));
+        rpp_gb::PathBatch paths{offsets, length, batch};
+        rpp_gb::StaticScratchRefusal refusal = rpp_gb::StaticScratchRefusal::None;
+        cudaError_t err;
+        if (dtype == RPP_GB_F64) {
+            if (int rc = check_signature_args<double>(plan, incr, offsets, length, sig, sig_stride, seed, seed_stride,
+                                                      grad, true))
+                return rc;
+            err = rpp_gb::launch_signature_static_scratch<double>(
+                plan->geometry, plan->device, s, static_cast<const double*>(incr), paths, static_cast<double*>(sig),
+                sig_stride, static_cast<const double*>(seed), seed_stride, static_cast<double*>(grad), threads,
+                &refusal);
+        } else {
+            if (int rc = check_signature_args<float>(plan, incr, offsets, length, sig, sig_stride, seed, seed_stride,
+                                                     grad, true))
+                return rc;
+            err = rpp_gb::launch_signature_static_scratch<float>(
+                plan->geometry, plan->device, s, static_cast<const float*>(incr), paths, static_cast<float*>(sig),
+                sig_stride, static_cast<const float*>(seed), seed_stride, static_cast<float*>(grad), threads,
+                &refusal);
+        }
+        if (refusal == rpp_gb::StaticScratchRefusal::BatchTooLarge)
+            return fail(RPP_GB_OUT_OF_BOUNDS, "ragged batch of " + std::to_string(batch) +
+                                                  " paths exceeds the static scratch capacity of " +
+                                                  std::to_string(rpp_gb::static_scratch_max_paths()) + " paths");
+        if (refusal == rpp_gb::StaticScratchRefusal::StateTooLarge)
+            return fail(RPP_GB_NOT_IMPLEMENTED,
+                        "signature state does not fit shared memory; this shape needs the global workspace of "
+                        "rpp_gb_signature");
+        return cuda_status(err, "signature kernel (static scratch)");
+    });
+}
+
 int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* incr,
                           const int64_t* offsets, int64_t length, int64_t batch, void* sig, int64_t sig_stride,
                           const void* seed, int64_t seed_stride, void* grad, int32_t* threads, float* ms) {

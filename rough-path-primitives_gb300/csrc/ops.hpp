@@ -90,4 +90,17 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
                              const T* seed, int64_t seed_stride, T* grad, bool forward, int threads);
 
+// Allocation-free signature launch: the ragged-batch scratch lives in a
+// fixed device array of the library (see signature.cu); refuses shapes whose
+// state needs the global-workspace kernel and batches beyond the array.
+enum class StaticScratchRefusal : int { None = 0, StateTooLarge = 1, BatchTooLarge = 2 };
+
+int64_t static_scratch_max_paths();
+
+template <typename T>
+cudaError_t launch_signature_static_scratch(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
+                                            const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
+                                            const T* seed, int64_t seed_stride, T* grad, int threads,
+                                            StaticScratchRefusal* refusal);
+
 }  // namespace rpp_gb

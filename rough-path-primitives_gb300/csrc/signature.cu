@@ -38,6 +38,8 @@
 // forward, the seed's top level in the reverse pass) | forward chains | 2 x
 // scaled increments | 1/m | one partial per thread | G levels 0..D-1 |
 // cotangent chains.
+#include <mutex>
+
 #include "common.cuh"
 #include "launch_util.cuh"
 #include "ops.hpp"
@@ -541,6 +543,100 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
     }
     return err;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant (rpp_gb_signature_static_scratch).
+//
+// Some callers cannot allocate device memory at call time: runtimes that own
+// the whole device memory through their own allocator (and forbid raw
+// cudaMalloc / cudaMallocAsync from plugins), real-time loops that must not
+// wait on or grow a memory pool, and hosts that budget device memory up front.
+// For them the ragged-batch scratch (the work counter and the longest-first
+// path order) lives in this fixed, file-scope device array instead of a
+// stream-ordered allocation.  Every GPU that loads the library holds the
+// array (8 MiB) until the process exits.  All calls share it and it keeps the
+// previous call's contents: the ordering kernel rewrites the order and zeroes
+// the counter on every call, and calls whose launches overlap on the GPU (on
+// different streams, or on one device from several threads without ordering)
+// race on it, so such calls must be serialised by the caller.  Host code only
+// holds a stand-in for the array's name; its device address is obtained once
+// per device, with that device current, by cudaGetSymbolAddress on the first
+// call made on that device (so that first call should come before any stream
+// capture).
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(8) << 20;
+static __device__ __align__(256) unsigned char g_signature_scratch[kStaticScratchBytes];
+
+std::mutex g_scratch_lock;
+void* g_scratch_address[kMaxDevices] = {};
+
+cudaError_t static_scratch_address(int device, void** out) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> guard(g_scratch_lock);
+    if (!g_scratch_address[device]) {
+        void* ptr = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&ptr, g_signature_scratch);
+        if (err != cudaSuccess) return err;
+        g_scratch_address[device] = ptr;
+    }
+    *out = g_scratch_address[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+int64_t static_scratch_max_paths() { return static_cast<int64_t>((kStaticScratchBytes - 256) / sizeof(int32_t)); }
+
+template <typename T>
+cudaError_t launch_signature_static_scratch(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const T* incr,
+                                            PathBatch paths, T* sig, int64_t sig_stride, const T* seed,
+                                            int64_t seed_stride, T* grad, int threads, StaticScratchRefusal* refusal) {
+    *refusal = StaticScratchRefusal::None;
+    if (paths.batch <= 0) return cudaSuccess;
+    const SigGeometry sg = make_sig_geometry(g);
+    int mode = kForward;
+    if (seed && grad) mode |= kBackward;
+    if (sig) mode |= kTopLevel;
+    // Only the shared-memory kernel: the global-workspace variant would need an allocation.
+    const int t = threads > 0 ? threads : threads_for(g.pw[g.depth]);
+    if (sig_smem_bytes<T>(sg, t, mode & kBackward, true) + 64 > static_cast<size_t>(dev.max_smem_optin)) {
+        *refusal = StaticScratchRefusal::StateTooLarge;
+        return cudaErrorNotSupported;
+    }
+    if (paths.offsets && paths.batch > 1) {
+        if (paths.batch > static_scratch_max_paths()) {
+            *refusal = StaticScratchRefusal::BatchTooLarge;
+            return cudaErrorNotSupported;
+        }
+        void* base = nullptr;
+        cudaError_t err = static_scratch_address(dev.device, &base);
+        if (err != cudaSuccess) return err;
+        paths.counter = static_cast<unsigned int*>(base);
+        paths.order = reinterpret_cast<int32_t*>(static_cast<char*>(base) + 256);
+        k_order_by_length<<<1, 1024, 0, s>>>(paths.offsets, paths.batch, const_cast<int32_t*>(paths.order),
+                                             paths.counter);
+        if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    }
+    switch (g.width) {
+        case 2: return launch_width<T, 2>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 3: return launch_width<T, 3>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 4: return launch_width<T, 4>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 5: return launch_width<T, 5>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 6: return launch_width<T, 6>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 8: return launch_width<T, 8>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 16: return launch_width<T, 16>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        default: return launch_width<T, 0>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+    }
+}
+
+template cudaError_t launch_signature_static_scratch<float>(const Geometry&, const DeviceInfo&, cudaStream_t,
+                                                            const float*, PathBatch, float*, int64_t, const float*,
+                                                            int64_t, float*, int, StaticScratchRefusal*);
+template cudaError_t launch_signature_static_scratch<double>(const Geometry&, const DeviceInfo&, cudaStream_t,
+                                                             const double*, PathBatch, double*, int64_t,
+                                                             const double*, int64_t, double*, int,
+                                                             StaticScratchRefusal*);
 
 template cudaError_t launch_signature<float>(const Geometry&, const DeviceInfo&, cudaStream_t, const float*,
                                              PathBatch, float*, int64_t, const float*, int64_t, float*, bool, int);

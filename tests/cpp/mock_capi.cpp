@@ -117,6 +117,10 @@ int rpp_gb_signature_backward(const rpp_gb_plan*, rpp_gb_stream, int32_t, const 
     return 0;
 }
 int rpp_gb_fma_peak(int32_t, int32_t, double*) { return 0; }
+int rpp_gb_signature_static_scratch(const rpp_gb_plan*, rpp_gb_stream, int32_t, const void*, const int64_t*, int64_t,
+                                    int64_t, void*, int64_t, const void*, int64_t, void*) {
+    return 0;
+}
 int rpp_gb_signature_tune(const rpp_gb_plan*, rpp_gb_stream, int32_t, const void*, const int64_t*, int64_t, int64_t,
                           void*, int64_t, const void*, int64_t, void*, int32_t*, float*) {
     return 0;

@@ -1,0 +1,92 @@
+"""The allocation-free signature entry point, rpp_gb_signature_static_scratch.
+
+It exists for callers that cannot allocate device memory while they run: a
+runtime that owns all device memory through its own allocator and does not
+let plugins call cudaMalloc or cudaMallocAsync, a real-time loop that must
+not wait on or grow a memory pool, a host that fixes its device-memory budget
+up front.  The entry point keeps the only scratch the signature launch needs
+(a ragged batch's work counter and longest-first order) in a fixed device
+array of the library, so it must give exactly what rpp_gb_signature gives.
+
+These tests call both entry points through the C ABI on the same ragged
+batch, twice in a row (the array keeps the previous call's contents, so the
+second call checks that each call re-initialises what it reads), and check
+that the entry point refuses what it cannot do without allocating.  This file
+is named to be collected last."""
+import ctypes
+import importlib
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+pkg = importlib.import_module("rough-path-primitives_gb300")
+
+F64 = 1
+
+
+def _ragged(rng, B, max_len, W):
+    lengths = rng.integers(0, max_len + 1, B)
+    offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    return offsets, rng.normal(0, 0.2, (int(offsets[-1]), W))
+
+
+def _call(name, plan, incr, offsets, B, sig, seed, grad, dim):
+    lib = pkg.library()
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = getattr(lib, name)(plan, stream, F64, incr.data_ptr(), offsets.data_ptr(), 0, B, sig.data_ptr(), dim,
+                            seed.data_ptr(), dim, grad.data_ptr())
+    msg = lib.rpp_gb_last_error_string()
+    return rc, (msg.decode() if msg else "")
+
+
+def test_static_scratch_matches_allocating_entry_on_two_calls():
+    W, D, B = 4, 4, 300
+    rng = np.random.default_rng(77)
+    offsets_h, incr_h = _ragged(rng, B, 64, W)
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    plan = basis.plan(0)
+    incr = torch.from_numpy(incr_h).cuda()
+    offsets = torch.from_numpy(offsets_h).cuda()
+    seed = torch.from_numpy(rng.uniform(-1, 1, (B, dim))).cuda()
+    sig_ref = torch.full((B, dim), float("nan"), dtype=torch.float64, device="cuda")
+    grad_ref = torch.full_like(incr, float("nan"))
+    rc, msg = _call("rpp_gb_signature", plan, incr, offsets, B, sig_ref, seed, grad_ref, dim)
+    assert rc == 0, msg
+    for call in range(2):
+        sig = torch.full_like(sig_ref, float("nan"))
+        grad = torch.full_like(grad_ref, float("nan"))
+        rc, msg = _call("rpp_gb_signature_static_scratch", plan, incr, offsets, B, sig, seed, grad, dim)
+        assert rc == 0, f"call {call}: {msg}"
+        torch.cuda.synchronize()
+        for got, want, what in ((sig, sig_ref, "signature"), (grad, grad_ref, "gradient")):
+            scale = torch.clamp(torch.maximum(got.abs(), want.abs()), min=1.0)
+            err = float(((got - want).abs() / scale).max())
+            assert err <= 1e-12, f"call {call} {what}: relative error {err:.3e}"
+
+
+def test_static_scratch_refuses_what_needs_an_allocation():
+    lib = pkg.library()
+    rng = np.random.default_rng(3)
+    offsets_h, incr_h = _ragged(rng, 4, 8, 6)
+    incr = torch.from_numpy(incr_h).cuda()
+    offsets = torch.from_numpy(offsets_h).cuda()
+    # a state that does not fit shared memory (width 6, depth 6, FP64)
+    big = pkg.TensorBasis(6, 6)
+    dim = big.size()
+    sig = torch.empty(4, dim, dtype=torch.float64, device="cuda")
+    seed = torch.zeros_like(sig)
+    grad = torch.empty_like(incr)
+    rc, msg = _call("rpp_gb_signature_static_scratch", big.plan(0), incr, offsets, 4, sig, seed, grad, dim)
+    assert rc == int(pkg.ErrorCode.NotImplemented) and "shared memory" in msg
+    # a ragged batch beyond the array's capacity is refused before any launch
+    small = pkg.TensorBasis(2, 2)
+    dim2 = small.size()
+    sig2 = torch.empty(1, dim2, dtype=torch.float64, device="cuda")
+    rc, msg = _call("rpp_gb_signature_static_scratch", small.plan(0), incr, offsets, 3_000_000, sig2,
+                    torch.zeros_like(sig2), torch.empty_like(incr), dim2)
+    assert rc == int(pkg.ErrorCode.OutOfBounds) and "capacity" in msg
+    assert ctypes.c_int(rc).value != 0
