@@ -19,8 +19,11 @@
  *    degree range is the view's (include/rpp/views/dense_graded_vector_view.hpp):
  *    coefficients outside it read as zero and are never written.
  *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
- *    asynchronous and stream-ordered; none synchronises the device and none
- *    allocates device memory after its plan / matrix handle is created.
+ *    asynchronous and stream-ordered and none synchronises the device.  The
+ *    per-operation entry points allocate nothing after their plan / matrix
+ *    handle is created; rpp_gb_signature allocates stream-ordered scratch
+ *    (cudaMallocAsync / cudaFreeAsync on `stream`) for ragged batches and for
+ *    states larger than shared memory.
  *  - dtype selects the scalar and accumulation type: RPP_GB_F32 (float data,
  *    float accumulation) or RPP_GB_F64 (double, double).
  */
