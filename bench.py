@@ -158,6 +158,238 @@ def plain_path(pkg, strat, cfg, basis, incr, ell, batch, grad):
     return prefixes[L]
 
 
+# ---------------------------------------------------------------------------
+# Other configurations (`--workload`), one JSON line each.  Device-resident
+# inputs; CUDA-event timing over `steps` launches after warm-up; FP64 peak
+# measured in-run; CPU baseline = the oracle on a bounded sample.
+# ---------------------------------------------------------------------------
+
+def _time_launches(torch, fn, steps, warmup, stream):
+    for _ in range(max(3, warmup)):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / steps
+
+
+def _fp64_peak(pkg, device):
+    import ctypes
+
+    out = ctypes.c_double(0)
+    rc = pkg.library().rpp_gb_fma_peak(1, device, ctypes.byref(out))
+    return out.value if rc == 0 else None
+
+
+def _line(metric, value, unit, ms, dtype, config, flops=None, peak=None, cpu=None, extra=None):
+    roof = None
+    if flops is not None and peak:
+        ach = flops / (ms / 1e3) / 1e12
+        roof = {"bound": "fp64_fma", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "traffic": None, "peak_source": "measured in-run (rpp_gb_fma_peak, FP64)",
+                "algorithmic_flops_per_launch": flops}
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "ms_per_step": ms,
+            "higher_is_better": True, "dtype": dtype, "data": "synthetic", "config": config, "roofline": roof,
+            "cpu_baseline": cpu}
+    if extra:
+        line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def workload_ft_mul(pkg, torch, args, peak):
+    """Plain batched ft_mul, W4 D4 (341 coefficients), FP64, batch 1024, U[-1,1]."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    W, D, B = 4, 4, 1024
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(torch.float64)
+    rng = np.random.default_rng(11)
+    lhs_h, rhs_h = rng.uniform(-1, 1, (B, dim)), rng.uniform(-1, 1, (B, dim))
+    lhs, rhs = torch.from_numpy(lhs_h).cuda(), torch.from_numpy(rhs_h).cuda()
+    out = torch.empty(B, dim, dtype=torch.float64, device="cuda")
+    mk = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
+    stream = torch.cuda.current_stream()
+    ms = 1e3 * _time_launches(torch, lambda: pkg.ft_mul(st, None, mk(out), mk(lhs), mk(rhs), basis, B),
+                              args.steps, args.warmup, stream)
+    fma = sum((k + 1) * W ** k for k in range(D + 1))
+    orc = O.Oracle()
+    e = np.zeros((B, dim))
+    t0 = time.perf_counter()
+    orc.ft_mul(W, D, e, lhs_h, rhs_h, ((0, D), (0, D), (0, D)))
+    cpu_s = time.perf_counter() - t0
+    err = float(np.max(np.abs(out.cpu().numpy() - e) / np.maximum(1, np.abs(e))))
+    _line("ft_mul products/sec (W4 D4 FP64, batch 1024)", B / (ms / 1e3), "products/s", ms, "f64",
+          {"workload": "ft_mul_w4_d4_b1024", "fma_per_product": fma, "bytes_per_product": 3 * dim * 8},
+          flops=2.0 * fma * B, peak=peak,
+          cpu={"value": B / cpu_s, "unit": "products/s", "cores": 1, "kind": "port", "sample": f"{B} products"},
+          extra={"parity": {"max_rel_err": err}})
+
+
+def workload_logsig(pkg, torch, args, peak):
+    """Log-signatures, W5 D5, 4096 paths of 256 steps: signature, ft_log,
+    tensor_to_lie (one SpMM launch, 829 Lie coefficients, nnz 10 517)."""
+    W, D, B, L = 5, 5, 4096, 256
+    basis, lbasis = pkg.TensorBasis(W, D), pkg.LieBasis(W, D)
+    dim, ts = basis.size(), lbasis.true_size()
+    st = pkg.GB300Strategy(torch.float64)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    incr = torch.randn(B * L, W, dtype=torch.float64, device="cuda", generator=g) / np.sqrt(L)
+    sig, log = (torch.empty(B, dim, dtype=torch.float64, device="cuda") for _ in range(2))
+    lie = torch.empty(B, ts, dtype=torch.float64, device="cuda")
+    t2l = pkg.make_t2l_matrix(lbasis)
+    full = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
+    lieb = pkg.make_lie_batch(lie, ts, 1, D)
+
+    def run():
+        pkg.signature(st, None, incr, basis, B, length=L, out=sig)
+        pkg.ft_log(st, None, full(log), full(sig), basis, B)
+        pkg.tensor_to_lie(st, None, lieb, full(log), lbasis, basis, B, t2l)
+
+    stream = torch.cuda.current_stream()
+    ms = 1e3 * _time_launches(torch, run, args.steps, args.warmup, stream)
+    log_fma = sum(sum(k * W ** k for k in range(1, m + 1)) for m in range(1, D + 1))
+    flops = 2.0 * B * (L * step_fma(W, D) + log_fma + t2l.nnz())
+    ms_sig = 1e3 * _time_launches(torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig),
+                                  args.steps, args.warmup, stream)
+    ms_log = 1e3 * _time_launches(torch, lambda: pkg.ft_log(st, None, full(log), full(sig), basis, B),
+                                  args.steps, args.warmup, stream)
+    ms_t2l = 1e3 * _time_launches(torch, lambda: pkg.tensor_to_lie(st, None, lieb, full(log), lbasis, basis, B, t2l),
+                                  args.steps, args.warmup, stream)
+    _line("log-signature paths/sec (W5 D5 L256 FP64): signature + ft_log + tensor_to_lie", B / (ms / 1e3),
+          "paths/s", ms, "f64", {"workload": "logsig_w5_d5_l256_b4096", "launches_per_step": 3},
+          flops=flops, peak=peak,
+          extra={"signature_only_ms": ms_sig, "ft_log_ms": ms_log, "tensor_to_lie_ms": ms_t2l,
+                 "ft_log_roofline_frac": 2.0 * B * log_fma / (ms_log / 1e3) / 1e12 / peak if peak else None,
+                 "tensor_to_lie_roofline_frac": 2.0 * B * t2l.nnz() / (ms_t2l / 1e3) / 1e12 / peak
+                 if peak else None})
+
+
+def workload_ragged(pkg, torch, args, peak):
+    """10,000 paths, lengths U{16..2048}, W8 D4, N(0, 1/len): one persistent
+    launch in FP64 and one in FP32, both replayed from one CUDA graph."""
+    W, D, B = 8, 4, 10_000
+    rng = np.random.default_rng(2024)
+    lengths = rng.integers(16, 2049, B)
+    offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    incr_h = rng.normal(0, 1, (offsets[-1], W)) / np.sqrt(np.repeat(lengths, lengths))[:, None]
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    off_d = torch.from_numpy(offsets).cuda()
+    x64 = torch.from_numpy(incr_h).cuda()
+    x32 = x64.float()
+    st64, st32 = pkg.GB300Strategy(torch.float64), pkg.GB300Strategy(torch.float32)
+    s64 = torch.empty(B, dim, dtype=torch.float64, device="cuda")
+    s32 = torch.empty(B, dim, dtype=torch.float32, device="cuda")
+    t64 = pkg.signature_tune(st64, None, x64, basis, B, offsets=off_d, out=s64)
+    t32 = pkg.signature_tune(st32, None, x32, basis, B, offsets=off_d, out=s32)
+    t64[0].raise_if_failed()
+    t32[0].raise_if_failed()
+
+    def run():
+        pkg.signature(st64, None, x64, basis, B, offsets=off_d, out=s64)
+        pkg.signature(st32, None, x32, basis, B, offsets=off_d, out=s32)
+
+    stream = torch.cuda.Stream()
+    run()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    stream.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            run()
+    torch.cuda.current_stream().wait_stream(stream)
+    cur = torch.cuda.current_stream()
+    ms = 1e3 * _time_launches(torch, graph.replay, args.steps, args.warmup, cur)
+    ms64 = 1e3 * _time_launches(torch, lambda: pkg.signature(st64, None, x64, basis, B, offsets=off_d, out=s64),
+                                args.steps, args.warmup, cur)
+    ms32 = 1e3 * _time_launches(torch, lambda: pkg.signature(st32, None, x32, basis, B, offsets=off_d, out=s32),
+                                args.steps, args.warmup, cur)
+    err32 = float(torch.max(torch.abs(s32.double() - s64) / torch.clamp(s64.abs(), min=1.0)).item())
+    steps_total = int(offsets[-1])
+    flops64 = 2.0 * steps_total * step_fma(W, D)
+    _line("uneven-length signatures paths/sec (W8 D4, 10k paths, L~U[16,2048]), FP64 + FP32 in one graph",
+          B / (ms / 1e3), "paths/s", ms, "f64+f32",
+          {"workload": "ragged_w8_d4_b10000", "total_increments": steps_total,
+           "graph": "fp64 launch + fp32 launch", "threads_per_cta": {"f64": t64[1], "f32": t32[1]}},
+          extra={"fp64_ms": ms64, "fp32_ms": ms32, "fp64_paths_per_s": B / (ms64 / 1e3),
+                 "fp32_paths_per_s": B / (ms32 / 1e3), "fp32_max_rel_err_vs_fp64": err32,
+                 "fp64_roofline_frac": flops64 / (ms64 / 1e3) / 1e12 / peak if peak else None})
+
+
+def workload_fwd_bwd(pkg, torch, args, peak, W, D, B, L, name):
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(torch.float64)
+    g = torch.Generator(device="cuda").manual_seed(W * 100 + D)
+    incr = torch.randn(B * L, W, dtype=torch.float64, device="cuda", generator=g) / np.sqrt(L)
+    ell = torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    sig = torch.empty(B, dim, dtype=torch.float64, device="cuda")
+    grad = torch.empty_like(incr)
+    err, threads, _ = pkg.signature_tune(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad)
+    err.raise_if_failed()
+    ms = 1e3 * _time_launches(
+        torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad),
+        args.steps, args.warmup, torch.cuda.current_stream())
+    _line(f"signature fwd+bwd paths/sec (W{W} D{D} L{L} FP64)", B / (ms / 1e3), "paths/s", ms, "f64",
+          {"workload": name, "batch": B, "length": L, "threads_per_cta": threads},
+          flops=2.0 * 4 * L * step_fma(W, D) * B, peak=peak)
+
+
+def workload_adjoints(pkg, torch, args, peak, W, D, B):
+    """Left and right adjoint multiplies by a random depth-truncated tensor."""
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(torch.float64)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    op, arg = (torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) - 0.5 for _ in range(2))
+    out = torch.empty_like(op)
+    mk = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
+    stream = torch.cuda.current_stream()
+    ms_l = 1e3 * _time_launches(torch, lambda: pkg.ft_adj_lmul(st, None, mk(out), mk(op), mk(arg), basis, B),
+                                args.steps, args.warmup, stream)
+    ms_r = 1e3 * _time_launches(torch, lambda: pkg.ft_adj_rmul(st, None, mk(out), mk(op), mk(arg), basis, B),
+                                args.steps, args.warmup, stream)
+    fma = sum(W ** m * W ** p for m in range(D + 1) for p in range(D + 1 - m))
+    _line(f"adjoint multiplies/sec (W{W} D{D} FP64, batch {B})", B / (ms_l / 1e3), "products/s", ms_l, "f64",
+          {"workload": f"adj_lmul_w{W}_d{D}_b{B}", "fma_per_product": fma}, flops=2.0 * fma * B, peak=peak,
+          extra={"adj_rmul_ms": ms_r, "adj_rmul_products_per_s": B / (ms_r / 1e3)})
+
+
+def run_workloads(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    pkg = importlib.import_module("rough-path-primitives_gb300")
+    peak = _fp64_peak(pkg, 0)
+    todo = args.workload.split(",")
+    if "all" in todo:
+        todo = ["ft_mul", "logsig", "ragged", "w6d6", "w2d12", "w16d3", "adjoints"]
+    for w in todo:
+        if w == "ft_mul":
+            workload_ft_mul(pkg, torch, args, peak)
+        elif w == "logsig":
+            workload_logsig(pkg, torch, args, peak)
+        elif w == "ragged":
+            workload_ragged(pkg, torch, args, peak)
+        elif w == "w6d6":
+            workload_fwd_bwd(pkg, torch, args, peak, 6, 6, 512, 128, "fwd_bwd_w6_d6_l128_b512")
+        elif w == "w2d12":
+            workload_fwd_bwd(pkg, torch, args, peak, 2, 12, 16384, 64, "fwd_bwd_w2_d12_l64_b16384")
+        elif w == "w16d3":
+            workload_fwd_bwd(pkg, torch, args, peak, 16, 3, 16384, 64, "fwd_bwd_w16_d3_l64_b16384")
+        elif w == "adjoints":
+            workload_adjoints(pkg, torch, args, peak, 2, 12, 16384)
+            workload_adjoints(pkg, torch, args, peak, 16, 3, 16384)
+        else:
+            raise SystemExit(f"unknown workload {w}")
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -185,9 +417,15 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-operation GPU comparator")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="paths per GPU (default: the headline 4096; smaller only for profiling captures)")
+    ap.add_argument("--workload", default=None,
+                    help="other configurations instead of the headline: ft_mul, logsig, ragged, w6d6, w2d12, "
+                         "w16d3, adjoints or all (comma-separated)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.workload:
+        run_workloads(args)
         return
 
     import torch
