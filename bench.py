@@ -361,6 +361,64 @@ def workload_adjoints(pkg, torch, args, peak, W, D, B):
           extra={"adj_rmul_ms": ms_r, "adj_rmul_products_per_s": B / (ms_r / 1e3)})
 
 
+def _binom(n, k):
+    c = 1
+    for i in range(1, k + 1):
+        c = c * (n - k + i) // i
+    return c
+
+
+def shuffle_terms(W, D):
+    """Algorithmic FMAs per tensor of each shuffle operation over full degree
+    ranges: one per (output coefficient, term) of the reference's sums."""
+    st = sum((2 * W) ** n for n in range(D + 1))
+    half = sum(W ** n * 2 ** (n - 1) for n in range(1, D + 1))
+    adj = sum(W ** n * _binom(n + m, m) * W ** m for n in range(D + 1) for m in range(D - n + 1))
+    hl = sum(W ** n * W * _binom(n + m, m) * W ** m for n in range(D) for m in range(D - n))
+    hr = sum(W ** n * _binom(n - 1 + m, m) * W ** m for n in range(1, D + 1) for m in range(D - n + 1))
+    return {"st_mul": st, "left_hs_mul": half, "st_adj_mul": adj, "left_hs_adj_lmul": hl, "left_hs_adj_rmul": hr}
+
+
+def workload_shuffle(pkg, torch, args, peak):
+    """Shuffle-algebra products and adjoints, W5 D5, batch 4096, FP64, U[-1/2,1/2]
+    operands (2 x 128 MB in, 128 MB out per launch: above L2), plus
+    tensor_pairing (HBM-bound)."""
+    W, D, B = 5, 5, 4096
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(torch.float64)
+    g = torch.Generator(device="cuda").manual_seed(17)
+    x, y = (torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) - 0.5 for _ in range(2))
+    out = torch.empty_like(x)
+    mk = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
+    stream = torch.cuda.current_stream()
+    terms = shuffle_terms(W, D)
+    for name in ("st_mul", "left_hs_mul", "st_adj_mul", "left_hs_adj_lmul", "left_hs_adj_rmul"):
+        fn = getattr(pkg, name)
+        ms = 1e3 * _time_launches(torch, lambda: fn(st, None, mk(out), mk(x), mk(y), basis, B), args.steps,
+                                  args.warmup, stream)
+        _line(f"{name} products/sec (W5 D5 FP64, batch 4096)", B / (ms / 1e3), "products/s", ms, "f64",
+              {"workload": f"{name}_w5_d5_b4096", "fma_per_product": terms[name]},
+              flops=2.0 * terms[name] * B, peak=peak)
+    res = torch.empty(B, dtype=torch.float64, device="cuda")
+    ms = 1e3 * _time_launches(torch, lambda: pkg.tensor_pairing(st, None, pkg.make_scalar_batch(res), mk(x), mk(y),
+                                                                basis, B), args.steps, args.warmup, stream)
+    nbytes = 2 * dim * 8 * B + 8 * B
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm = float(json.load(f)["hbm_gbs"])
+        src = "MEASURED_PEAKS.json hbm_gbs"
+    except (OSError, KeyError, ValueError):
+        hbm, src = 6800.0, "fallback"
+    ach = nbytes / (ms / 1e3) / 1e9
+    print(json.dumps({"metric": "tensor_pairing pairs/sec (W5 D5 FP64, batch 4096)", "value": B / (ms / 1e3),
+                      "unit": "pairs/s", "n_gpus": 1, "ms_per_step": ms, "higher_is_better": True, "dtype": "f64",
+                      "data": "synthetic", "config": {"workload": "tensor_pairing_w5_d5_b4096",
+                                                      "bytes_per_pair": 2 * dim * 8 + 8},
+                      "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                                   "frac": ach / hbm, "traffic": None, "peak_source": src}}), flush=True)
+
+
 def run_workloads(args):
     import torch
 
@@ -369,7 +427,7 @@ def run_workloads(args):
     peak = _fp64_peak(pkg, 0)
     todo = args.workload.split(",")
     if "all" in todo:
-        todo = ["ft_mul", "logsig", "ragged", "w6d6", "w2d12", "w16d3", "adjoints"]
+        todo = ["ft_mul", "logsig", "ragged", "w6d6", "w2d12", "w16d3", "adjoints", "shuffle"]
     for w in todo:
         if w == "ft_mul":
             workload_ft_mul(pkg, torch, args, peak)
@@ -383,6 +441,8 @@ def run_workloads(args):
             workload_fwd_bwd(pkg, torch, args, peak, 2, 12, 16384, 64, "fwd_bwd_w2_d12_l64_b16384")
         elif w == "w16d3":
             workload_fwd_bwd(pkg, torch, args, peak, 16, 3, 16384, 64, "fwd_bwd_w16_d3_l64_b16384")
+        elif w == "shuffle":
+            workload_shuffle(pkg, torch, args, peak)
         elif w == "adjoints":
             workload_adjoints(pkg, torch, args, peak, 2, 12, 16384)
             workload_adjoints(pkg, torch, args, peak, 16, 3, 16384)
@@ -419,7 +479,7 @@ def main():
                     help="paths per GPU (default: the headline 4096; smaller only for profiling captures)")
     ap.add_argument("--workload", default=None,
                     help="other configurations instead of the headline: ft_mul, logsig, ragged, w6d6, w2d12, "
-                         "w16d3, adjoints or all (comma-separated)")
+                         "w16d3, adjoints, shuffle or all (comma-separated)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)

@@ -180,6 +180,72 @@ int rpp_gb_tensor_add_identity(const rpp_gb_plan* plan, rpp_gb_stream stream, in
                                const rpp_gb_tensor_arg* out, int64_t batch, double scalar);
 
 /* ------------------------------------------------------------------------
+ * Shuffle algebra and the tensor pairing.  A coefficient of degree n of a
+ * shuffle product sums 2^n terms (word_shuffle_product.hpp:43-97); terms whose
+ * factors lie outside an operand's degree range are omitted, never read.
+ * ---------------------------------------------------------------------- */
+
+/* rpp::ops::st_mul (include/rpp/operations/basic/st_mul.hpp:53-79):
+ * out = beta * lhs sh rhs on out's degree range. */
+int rpp_gb_st_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                  const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* lhs,
+                  const rpp_gb_tensor_arg* rhs, int64_t batch, double beta);
+
+/* rpp::ops::st_fma (include/rpp/operations/basic/st_fma.hpp:56-85):
+ * out = alpha*a + beta * b sh c. */
+int rpp_gb_st_fma(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                  const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* a,
+                  const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c, int64_t batch,
+                  double alpha, double beta);
+
+/* rpp::ops::st_inplace_fma (include/rpp/operations/basic/st_inplace_fma.hpp:
+ * 50-80): a <- alpha*a + beta * b sh c.  a must not overlap b or c. */
+int rpp_gb_st_inplace_fma(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                          const rpp_gb_tensor_arg* a, const rpp_gb_tensor_arg* b,
+                          const rpp_gb_tensor_arg* c, int64_t batch, double alpha, double beta);
+
+/* rpp::ops::st_adj_mul (include/rpp/operations/basic/st_adj_mul.hpp:46-69):
+ * the adjoint of x -> op sh x, out[w] = sum_u op[u] sum_{s in w sh u} arg[s].
+ * Every coefficient of out's range is written (zero when no term exists). */
+int rpp_gb_st_adj_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                      const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op,
+                      const rpp_gb_tensor_arg* arg, int64_t batch);
+
+/* rpp::ops::left_hs_mul (include/rpp/operations/basic/left_hs_mul.hpp:59-87):
+ * out = beta * integrator < integrand (left half-shuffle; the first letter
+ * of every word comes from the integrator), out[0] = 0. */
+int rpp_gb_left_hs_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                       const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* integrator,
+                       const rpp_gb_tensor_arg* integrand, int64_t batch, double beta);
+
+/* rpp::ops::left_hs_adj_lmul (include/rpp/operations/basic/
+ * left_hs_adj_lmul.hpp:39-57): the adjoint of y -> x < y with x = op (the
+ * integrator) fixed and arg the cotangent:
+ * out[w] = beta * sum_a sum_u op[a u] sum_{s in w sh u} arg[a s].
+ * beta scales the result as in the reference's block strategy (its CPU
+ * strategy takes no scale: beta = 1). */
+int rpp_gb_left_hs_adj_lmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                            const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op,
+                            const rpp_gb_tensor_arg* arg, int64_t batch, double beta);
+
+/* rpp::ops::left_hs_adj_rmul (include/rpp/operations/basic/
+ * left_hs_adj_rmul.hpp:39-57): the adjoint of x -> x < y with op the
+ * cotangent (integrator slot) and arg = y (the integrand) fixed:
+ * out[a v] = beta * sum_u arg[u] sum_{s in v sh u} op[a s], out[0] = 0. */
+int rpp_gb_left_hs_adj_rmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                            const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op,
+                            const rpp_gb_tensor_arg* arg, int64_t batch, double beta);
+
+/* rpp::ops::tensor_pairing (include/rpp/operations/basic/tensor_pairing.hpp:
+ * 47-73): result[b] = sum of functional[i] arg[i] over the degrees both views
+ * hold (0 when they share none).  `result` is a device array of `batch`
+ * contiguous scalars of dtype (rpp::make_scalar_batch,
+ * include/rpp/views/scalar_view.hpp:53-60). */
+int rpp_gb_tensor_pairing(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                          void* result, const rpp_gb_tensor_arg* functional,
+                          const rpp_gb_tensor_arg* arg, int64_t batch);
+
+/* ------------------------------------------------------------------------
  * Sparse matrices and the Lie <-> tensor conversions.
  * ---------------------------------------------------------------------- */
 

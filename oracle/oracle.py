@@ -94,6 +94,11 @@ class Oracle:
         vp = ctypes.c_void_p
         L.orc_spmv.argtypes = [i64, ctypes.c_int, i64, vp, vp, vp, vp, i64, i64, i64, vp, i64, i64, dbl]
         L.orc_signature.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, i32]
+        L.orc_st.argtypes = [i32, i32, i64, ctypes.c_int, P, P, P, P, dbl, dbl]
+        L.orc_left_hs_mul.argtypes = [i32, i32, i64, P, P, P, dbl]
+        L.orc_st_adj_mul.argtypes = [i32, i32, i64, P, P, P]
+        L.orc_left_hs_adjoint.argtypes = [i32, i32, i64, ctypes.c_int, P, P, P, dbl]
+        L.orc_tensor_pairing.argtypes = [i32, i32, i64, vp, P, P]
 
     @staticmethod
     def _p(x):
@@ -175,6 +180,50 @@ class Oracle:
                                None if grad is None else grad.ctypes.data, threads)
         return sig, grad
 
+
+
+    # -- shuffle algebra -------------------------------------------------
+    def _st(self, W, D, mode, out, a, b, c, ranges, alpha, beta):
+        n, s = out.shape
+        return self.lib.orc_st(W, D, n, mode, self._p(_arg(out, s, ranges[0])), self._p(_arg(a, s, ranges[1])),
+                               self._p(_arg(b, s, ranges[2])), self._p(_arg(c, s, ranges[3])), alpha, beta)
+
+    def st_mul(self, W, D, out, lhs, rhs, ranges, beta=1.0):
+        """out = beta * lhs sh rhs.  ranges = (out, lhs, rhs)."""
+        self._st(W, D, 0, out, None, lhs, rhs, (ranges[0], (1, 0), ranges[1], ranges[2]), 0.0, beta)
+
+    def st_fma(self, W, D, out, a, b, c, ranges, alpha=1.0, beta=1.0):
+        """out = alpha*a + beta * b sh c.  ranges = (out, a, b, c)."""
+        self._st(W, D, 1, out, a, b, c, ranges, alpha, beta)
+
+    def st_inplace_fma(self, W, D, a, b, c, ranges, alpha=1.0, beta=1.0):
+        """a = alpha*a + beta * b sh c.  ranges = (a, b, c)."""
+        self._st(W, D, 2, a, None, b, c, (ranges[0], (1, 0), ranges[1], ranges[2]), alpha, beta)
+
+    def left_hs_mul(self, W, D, out, integrator, integrand, ranges, beta=1.0):
+        n, s = out.shape
+        self.lib.orc_left_hs_mul(W, D, n, self._p(_arg(out, s, ranges[0])), self._p(_arg(integrator, s, ranges[1])),
+                                 self._p(_arg(integrand, s, ranges[2])), beta)
+
+    def st_adj_mul(self, W, D, out, op, arg, ranges):
+        n, s = out.shape
+        self.lib.orc_st_adj_mul(W, D, n, self._p(_arg(out, s, ranges[0])), self._p(_arg(op, s, ranges[1])),
+                                self._p(_arg(arg, s, ranges[2])))
+
+    def left_hs_adjoint(self, W, D, lmul, out, integrator, integrand, ranges, beta=1.0):
+        """lmul: (out, fixed integrator, integrand cotangent); rmul: (out,
+        integrator cotangent, fixed integrand) -- the reference operator's order."""
+        n, s = out.shape
+        self.lib.orc_left_hs_adjoint(W, D, n, int(lmul), self._p(_arg(out, s, ranges[0])),
+                                     self._p(_arg(integrator, s, ranges[1])),
+                                     self._p(_arg(integrand, s, ranges[2])), beta)
+
+    def tensor_pairing(self, W, D, functional, arg, ranges):
+        n, s = functional.shape
+        res = np.zeros(n)
+        self.lib.orc_tensor_pairing(W, D, n, res.ctypes.data, self._p(_arg(functional, s, ranges[0])),
+                                    self._p(_arg(arg, s, ranges[1])))
+        return res
 
 # ---------------------------------------------------------------------------
 # Hall basis, bracket expansions and the tensor <-> Lie conversion matrices.
@@ -391,6 +440,11 @@ class RefBridge(Oracle):
         L.ref_conversion_matrix.restype = i64
         L.ref_tensor_lie.argtypes = [i32, i32, i64, ctypes.c_int, i64, i64, i64, vp, vp, vp, vp, i64, vp, i64]
         L.ref_signature.argtypes = [i32, i32, i64, vp, vp, vp, i32]
+        L.ref_st.argtypes = [i32, i32, i64, ctypes.c_int, P, P, P, P, dbl, dbl]
+        L.ref_st_adj_mul.argtypes = [i32, i32, i64, P, P, P]
+        L.ref_left_hs_mul.argtypes = [i32, i32, i64, P, P, P, dbl]
+        L.ref_left_hs_adjoint.argtypes = [i32, i32, i64, ctypes.c_int, P, P, P]
+        L.ref_tensor_pairing.argtypes = [i32, i32, i64, vp, P, P]
 
     def _chk(self, rc):
         if rc != 0:
@@ -482,3 +536,34 @@ class RefBridge(Oracle):
         sig = np.zeros((B, tensor_dim(W, D)))
         self._chk(self.lib.ref_signature(W, D, B, incr.ctypes.data, offsets.ctypes.data, sig.ctypes.data, threads))
         return sig, None
+
+    def _st(self, W, D, mode, out, a, b, c, ranges, alpha, beta):
+        n, s = out.shape
+        self._chk(self.lib.ref_st(W, D, n, mode, self._p(_arg(out, s, ranges[0])), self._p(_arg(a, s, ranges[1])),
+                                  self._p(_arg(b, s, ranges[2])), self._p(_arg(c, s, ranges[3])), alpha, beta))
+
+    def left_hs_mul(self, W, D, out, integrator, integrand, ranges, beta=1.0):
+        n, s = out.shape
+        self._chk(self.lib.ref_left_hs_mul(W, D, n, self._p(_arg(out, s, ranges[0])),
+                                           self._p(_arg(integrator, s, ranges[1])),
+                                           self._p(_arg(integrand, s, ranges[2])), beta))
+
+    def st_adj_mul(self, W, D, out, op, arg, ranges):
+        n, s = out.shape
+        self._chk(self.lib.ref_st_adj_mul(W, D, n, self._p(_arg(out, s, ranges[0])), self._p(_arg(op, s, ranges[1])),
+                                          self._p(_arg(arg, s, ranges[2]))))
+
+    def left_hs_adjoint(self, W, D, lmul, out, integrator, integrand, ranges, beta=1.0):
+        """The reference's CPU operators take no scale factor: beta must be 1."""
+        assert beta == 1.0
+        n, s = out.shape
+        self._chk(self.lib.ref_left_hs_adjoint(W, D, n, int(lmul), self._p(_arg(out, s, ranges[0])),
+                                               self._p(_arg(integrator, s, ranges[1])),
+                                               self._p(_arg(integrand, s, ranges[2]))))
+
+    def tensor_pairing(self, W, D, functional, arg, ranges):
+        n, s = functional.shape
+        res = np.full(n, np.nan)
+        self._chk(self.lib.ref_tensor_pairing(W, D, n, res.ctypes.data, self._p(_arg(functional, s, ranges[0])),
+                                              self._p(_arg(arg, s, ranges[1]))))
+        return res

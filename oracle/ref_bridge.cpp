@@ -261,4 +261,60 @@ int ref_signature(int32_t W, int32_t D, int64_t n, double const* incr, int64_t c
     return 0;
 }
 
+// Shuffle algebra through the public front ends (include/rpp/operations/basic/
+// st_mul.hpp, st_fma.hpp, st_inplace_fma.hpp, st_adj_mul.hpp, left_hs_mul.hpp,
+// tensor_pairing.hpp).  mode 0: st_mul(out, b, c, beta); 1: st_fma(out, a, b,
+// c, alpha, beta); 2: st_inplace_fma(out, b, c, alpha, beta).
+int ref_st(int32_t W, int32_t D, int64_t n, int mode, Arg const* out, Arg const* a, Arg const* b,
+           Arg const* c, double alpha, double beta) {
+    BasisData bd(W, D);
+    if (mode == 0)
+        return status(rpp::ops::st_mul(Strategy{}, {}, batch(out), cbatch(b), cbatch(c), bd.basis, n, beta));
+    if (mode == 1)
+        return status(rpp::ops::st_fma(Strategy{}, {}, batch(out), cbatch(a), cbatch(b), cbatch(c), bd.basis,
+                                       n, alpha, beta));
+    return status(
+        rpp::ops::st_inplace_fma(Strategy{}, {}, batch(out), cbatch(b), cbatch(c), bd.basis, n, alpha, beta));
+}
+
+int ref_st_adj_mul(int32_t W, int32_t D, int64_t n, Arg const* out, Arg const* op, Arg const* arg) {
+    BasisData bd(W, D);
+    return status(rpp::ops::st_adj_mul(Strategy{}, {}, batch(out), cbatch(op), cbatch(arg), bd.basis, n));
+}
+
+int ref_left_hs_mul(int32_t W, int32_t D, int64_t n, Arg const* out, Arg const* x, Arg const* y,
+                    double beta) {
+    BasisData bd(W, D);
+    return status(rpp::ops::left_hs_mul(Strategy{}, {}, batch(out), cbatch(x), cbatch(y), bd.basis, n, beta));
+}
+
+// The CPU strategy's half-shuffle adjoints take no scale factor, so they are
+// driven through their operation objects, as the reference's own tests do
+// (tests/rpp/cpu/single_thread/ops/left_hs_adjoint_tests.cpp:29-56):
+// (out, integrator, integrand) in the operator's argument order.
+int ref_left_hs_adjoint(int32_t W, int32_t D, int64_t n, int lmul, Arg const* out, Arg const* integrator,
+                        Arg const* integrand) {
+    BasisData bd(W, D);
+    const Strategy::Context ctx(nullptr);
+    for (int64_t b = 0; b < n; ++b) {
+        rpp::DenseTensorView<double*, Basis> o(out->data + b * out->stride, bd.basis, Degree{out->min_degree},
+                                          Degree{out->max_degree});
+        rpp::DenseTensorView<double const*, Basis> x(integrator->data + b * integrator->stride, bd.basis,
+                                                Degree{integrator->min_degree}, Degree{integrator->max_degree});
+        rpp::DenseTensorView<double const*, Basis> y(integrand->data + b * integrand->stride, bd.basis,
+                                                Degree{integrand->min_degree}, Degree{integrand->max_degree});
+        if (lmul)
+            rpp::ops::LeftHSAdjLMul<Strategy>{ctx, rpp::basis::make_basis_pack(bd.basis)}(ctx, o, x, y);
+        else
+            rpp::ops::LeftHSAdjRMul<Strategy>{ctx, rpp::basis::make_basis_pack(bd.basis)}(ctx, o, x, y);
+    }
+    return 0;
+}
+
+int ref_tensor_pairing(int32_t W, int32_t D, int64_t n, double* result, Arg const* f, Arg const* a) {
+    BasisData bd(W, D);
+    return status(rpp::ops::tensor_pairing(Strategy{}, {}, rpp::make_scalar_batch(result), cbatch(f), cbatch(a),
+                                           bd.basis, n));
+}
+
 }  // extern "C"

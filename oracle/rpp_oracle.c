@@ -563,3 +563,214 @@ int orc_signature(int32_t W, int32_t D, int64_t batch, const double* incr, const
     for (int t = 0; t < started; ++t) pthread_join(tid[t], NULL);
     return 0;
 }
+
+/* ---------------------------------------------------------------------------
+ * Shuffle algebra.  Each coefficient is enumerated over subsets of letter
+ * positions, first letter first, the way the reference's own test references
+ * do (tests/rpp/shuffle_adjoint_test_helper.hpp:49-94 and
+ * tests/rpp/half_shuffle_adjoint_test_helper.hpp:12-80), independently of
+ * the operation's masked index packing.
+ * ------------------------------------------------------------------------- */
+
+/* Letters of a level index, first letter first. */
+static void word_letters(const orc_basis* B, int32_t n, int64_t idx, int32_t* w) {
+    for (int32_t p = n - 1; p >= 0; --p) {
+        w[p] = (int32_t)(idx % B->width);
+        idx /= B->width;
+    }
+}
+
+/* Split the word w (n letters) by the position subset `mask` (bit p = letter
+ * p, first letter = bit 0): the letters in the subset form `sel`, the others
+ * `rest`, both in order.  Returns |sel|. */
+static int32_t split_word(const orc_basis* B, const int32_t* w, int32_t n, uint64_t mask,
+                          int64_t* sel, int64_t* rest) {
+    int32_t k = 0;
+    *sel = 0;
+    *rest = 0;
+    for (int32_t p = 0; p < n; ++p) {
+        if ((mask >> p) & 1u) {
+            *sel = *sel * B->width + w[p];
+            ++k;
+        } else {
+            *rest = *rest * B->width + w[p];
+        }
+    }
+    return k;
+}
+
+/* (lhs sh rhs)[w] = sum over position subsets S of lhs[w|S] rhs[w|S^c], terms
+ * whose degrees fall outside an operand's range omitted
+ * (operations/implementation/word_shuffle_product.hpp:43-97).  With
+ * `half`, position 0 always goes to lhs: the left half-shuffle coefficient
+ * (operations/implementation/word_half_shuffle_product.hpp:12-56). */
+static double shuffle_coeff(const orc_basis* B, int32_t n, int64_t idx, const double* lhs,
+                            int32_t lmin, int32_t lmax, const double* rhs, int32_t rmin,
+                            int32_t rmax, int half) {
+    int32_t w[ORC_MAX_DEPTH];
+    word_letters(B, n, idx, w);
+    double acc = 0.0;
+    for (uint64_t mask = 0; mask < ((uint64_t)1 << n); ++mask) {
+        if (half && !(mask & 1u)) continue;
+        int64_t li, ri;
+        int32_t kl = split_word(B, w, n, mask, &li, &ri);
+        int32_t kr = n - kl;
+        if (!in_range(kl, lmin, lmax) || !in_range(kr, rmin, rmax)) continue;
+        acc += lhs[B->db[kl] + li] * rhs[B->db[kr] + ri];
+    }
+    return acc;
+}
+
+/* cpu/single_thread/operations/basic/st_mul.hpp:44-69 (mode 0: out = beta
+ * lhs sh rhs), st_fma.hpp:44-80 (mode 1: out = alpha a + beta b sh c) and
+ * st_inplace_fma.hpp:44-70 (mode 2: a = alpha a + beta b sh c, `out` is a). */
+static void one_st(const orc_basis* B, int mode, double* out, int32_t omin, int32_t omax,
+                   const double* a, int32_t amin, int32_t amax, const double* b, int32_t bmin,
+                   int32_t bmax, const double* c, int32_t cmin, int32_t cmax, double alpha,
+                   double beta) {
+    for (int32_t n = omin; n <= omax && n <= B->depth; ++n) {
+        for (int64_t i = 0; i < B->pw[n]; ++i) {
+            double prod = shuffle_coeff(B, n, i, b, bmin, bmax, c, cmin, cmax, 0);
+            double v = beta * prod;
+            if (mode == 1 && a && in_range(n, amin, amax)) v += alpha * a[B->db[n] + i];
+            if (mode == 2) v += alpha * out[B->db[n] + i];
+            out[B->db[n] + i] = v;
+        }
+    }
+}
+
+/* cpu/single_thread/operations/basic/left_hs_mul.hpp:44-84: out[0] = 0 and
+ * out[a v] = beta (integrator < integrand)[a v]. */
+static void one_left_hs_mul(const orc_basis* B, double* out, int32_t omin, int32_t omax,
+                            const double* x, int32_t xmin, int32_t xmax, const double* y,
+                            int32_t ymin, int32_t ymax, double beta) {
+    for (int32_t n = omin; n <= omax && n <= B->depth; ++n) {
+        for (int64_t i = 0; i < B->pw[n]; ++i)
+            out[B->db[n] + i] = n == 0 ? 0.0 : beta * shuffle_coeff(B, n, i, x, xmin, xmax, y, ymin, ymax, 1);
+    }
+}
+
+/* cpu/single_thread/operations/basic/st_adj_mul.hpp:46-85 with
+ * operations/implementation/shuffle_adjoint_op_loop.hpp and
+ * word_shuffle_adjoint_multiply.hpp: out[w] = sum_u op[u] sum_{s in w sh u}
+ * arg[s], i.e. <out, x> = <arg, op sh x>.  Written as the transpose of the
+ * shuffle product: every arg word s and position subset S send
+ * op[s|S] arg[s] to out[s|S^c]. */
+static void one_st_adj_mul(const orc_basis* B, double* out, int32_t omin, int32_t omax,
+                           const double* op, int32_t pmin, int32_t pmax, const double* arg,
+                           int32_t amin, int32_t amax) {
+    one_set_zero(B, out, omin, omax);
+    int32_t w[ORC_MAX_DEPTH];
+    for (int32_t N = amin; N <= amax && N <= B->depth; ++N) {
+        for (int64_t s = 0; s < B->pw[N]; ++s) {
+            word_letters(B, N, s, w);
+            for (uint64_t mask = 0; mask < ((uint64_t)1 << N); ++mask) {
+                int64_t pi, oi;
+                int32_t kp = split_word(B, w, N, mask, &pi, &oi);
+                int32_t ko = N - kp;
+                if (!in_range(kp, pmin, pmax) || !in_range(ko, omin, omax)) continue;
+                out[B->db[ko] + oi] += op[B->db[kp] + pi] * arg[B->db[N] + s];
+            }
+        }
+    }
+}
+
+/* The adjoints of the left half-shuffle x < y with respect to each factor,
+ * as the transpose of the forward product: every arg word s (degree >= 1)
+ * and split of its positions 1.. into (left rest, right) with position 0
+ * on the left.
+ *   fixed_left  (cpu/single_thread/operations/basic/left_hs_adj_lmul.hpp:
+ *               73-124): out = y-cotangent, out[right] += beta x[left] arg[s]
+ *               with x = `fixed` (the integrator) and arg = the integrand
+ *               cotangent;
+ *   !fixed_left (left_hs_adj_rmul.hpp:44-106): out = x-cotangent,
+ *               out[left] += beta y[right] arg[s] with y = `fixed` (the
+ *               integrand) and arg = the integrator cotangent; out[0] = 0. */
+static void one_left_hs_adjoint(const orc_basis* B, int fixed_left, double* out, int32_t omin,
+                                int32_t omax, const double* fixed, int32_t fmin, int32_t fmax,
+                                const double* arg, int32_t amin, int32_t amax, double beta) {
+    one_set_zero(B, out, omin, omax);
+    int32_t w[ORC_MAX_DEPTH];
+    for (int32_t N = imax(amin, 1); N <= amax && N <= B->depth; ++N) {
+        for (int64_t s = 0; s < B->pw[N]; ++s) {
+            word_letters(B, N, s, w);
+            for (uint64_t mask = 1; mask < ((uint64_t)1 << N); mask += 2) {
+                int64_t li, ri;
+                int32_t kl = split_word(B, w, N, mask, &li, &ri);
+                int32_t kr = N - kl;
+                int32_t kf = fixed_left ? kl : kr, ko = fixed_left ? kr : kl;
+                int64_t fi = fixed_left ? li : ri, oi = fixed_left ? ri : li;
+                if (!in_range(kf, fmin, fmax) || !in_range(ko, omin, omax)) continue;
+                out[B->db[ko] + oi] += beta * fixed[B->db[kf] + fi] * arg[B->db[N] + s];
+            }
+        }
+    }
+}
+
+int orc_st(int32_t W, int32_t D, int64_t batch, int mode, const orc_arg* out, const orc_arg* a,
+           const orc_arg* b, const orc_arg* c, double alpha, double beta) {
+    orc_basis B;
+    basis_init(&B, W, D);
+    for (int64_t k = 0; k < batch; ++k)
+        one_st(&B, mode, ORC_PTR(out, k), out->min_degree, out->max_degree, a ? ORC_PTR(a, k) : NULL,
+               a ? a->min_degree : 1, a ? a->max_degree : 0, ORC_PTR(b, k), b->min_degree,
+               b->max_degree, ORC_PTR(c, k), c->min_degree, c->max_degree, alpha, beta);
+    return 0;
+}
+
+int orc_left_hs_mul(int32_t W, int32_t D, int64_t batch, const orc_arg* out, const orc_arg* x,
+                    const orc_arg* y, double beta) {
+    orc_basis B;
+    basis_init(&B, W, D);
+    for (int64_t k = 0; k < batch; ++k)
+        one_left_hs_mul(&B, ORC_PTR(out, k), out->min_degree, out->max_degree, ORC_PTR(x, k),
+                        x->min_degree, x->max_degree, ORC_PTR(y, k), y->min_degree, y->max_degree,
+                        beta);
+    return 0;
+}
+
+int orc_st_adj_mul(int32_t W, int32_t D, int64_t batch, const orc_arg* out, const orc_arg* op,
+                   const orc_arg* arg) {
+    orc_basis B;
+    basis_init(&B, W, D);
+    for (int64_t k = 0; k < batch; ++k)
+        one_st_adj_mul(&B, ORC_PTR(out, k), out->min_degree, out->max_degree, ORC_PTR(op, k),
+                       op->min_degree, op->max_degree, ORC_PTR(arg, k), arg->min_degree,
+                       arg->max_degree);
+    return 0;
+}
+
+/* lmul: (out, integrator, integrand) = (out, fixed x, cotangent);
+ * rmul: (out, integrator, integrand) = (out, cotangent, fixed y) -- the
+ * argument order of the reference's operator() in both cases. */
+int orc_left_hs_adjoint(int32_t W, int32_t D, int64_t batch, int lmul, const orc_arg* out,
+                        const orc_arg* integrator, const orc_arg* integrand, double beta) {
+    orc_basis B;
+    basis_init(&B, W, D);
+    const orc_arg* fixed = lmul ? integrator : integrand;
+    const orc_arg* cot = lmul ? integrand : integrator;
+    for (int64_t k = 0; k < batch; ++k)
+        one_left_hs_adjoint(&B, lmul, ORC_PTR(out, k), out->min_degree, out->max_degree,
+                            ORC_PTR(fixed, k), fixed->min_degree, fixed->max_degree, ORC_PTR(cot, k),
+                            cot->min_degree, cot->max_degree, beta);
+    return 0;
+}
+
+/* cpu/single_thread/operations/basic/tensor_pairing.hpp:40-72: result[b] =
+ * sum of functional[i] arg[i] over the degrees both views hold. */
+int orc_tensor_pairing(int32_t W, int32_t D, int64_t batch, double* result, const orc_arg* f,
+                       const orc_arg* a) {
+    orc_basis B;
+    basis_init(&B, W, D);
+    int32_t lo = imax(f->min_degree, a->min_degree);
+    int32_t hi = imin(imin(f->max_degree, a->max_degree), D);
+    for (int64_t k = 0; k < batch; ++k) {
+        const double* fp = ORC_PTR(f, k);
+        const double* ap = ORC_PTR(a, k);
+        double acc = 0.0;
+        if (lo <= hi)
+            for (int64_t i = B.db[lo]; i < B.db[hi + 1]; ++i) acc += fp[i] * ap[i];
+        result[k] = acc;
+    }
+    return 0;
+}

@@ -31,7 +31,9 @@ __all__ = [
     "ft_fmexp", "ft_log", "ft_adj_lmul", "ft_adj_rmul", "tensor_antipode", "tensor_reflect",
     "tensor_generalised_antipode", "vector_assign", "vector_set_constant",
     "tensor_set_identity", "tensor_add_identity", "sparse_matrix_vector_product",
-    "tensor_to_lie", "lie_to_tensor", "signature", "signature_backward", "signature_tune", "exp_letter_vjp", "build", "library",
+    "tensor_to_lie", "lie_to_tensor", "signature", "signature_backward", "signature_tune", "exp_letter_vjp",
+    "st_mul", "st_fma", "st_inplace_fma", "st_adj_mul", "left_hs_mul", "left_hs_adj_lmul", "left_hs_adj_rmul",
+    "tensor_pairing", "make_scalar_batch", "build", "library",
 ]
 
 
@@ -361,6 +363,95 @@ def ft_adj_rmul(strategy, config, out, op, arg, basis, num_batches) -> Error:
     lib = _lib.load()
     return _status(lib.rpp_gb_ft_adj_rmul(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
                                           strategy.dtype_code(), _p(out), _p(op), _p(arg), num_batches))
+
+
+# --------------------------------------------------------------------------
+# Shuffle algebra and the tensor pairing.
+# --------------------------------------------------------------------------
+
+def st_mul(strategy, config, out, lhs, rhs, basis, num_batches, beta=1.0) -> Error:
+    """include/rpp/operations/basic/st_mul.hpp:53-79: out = beta * lhs sh rhs."""
+    _check_batches(strategy, out, lhs, rhs)
+    lib = _lib.load()
+    return _status(lib.rpp_gb_st_mul(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
+                                     strategy.dtype_code(), _p(out), _p(lhs), _p(rhs), num_batches, beta))
+
+
+def st_fma(strategy, config, out, a, b, c, basis, num_batches, alpha=1.0, beta=1.0) -> Error:
+    """include/rpp/operations/basic/st_fma.hpp:56-85: out = alpha*a + beta * b sh c."""
+    _check_batches(strategy, out, a, b, c)
+    lib = _lib.load()
+    return _status(lib.rpp_gb_st_fma(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
+                                     strategy.dtype_code(), _p(out), _p(a), _p(b), _p(c), num_batches,
+                                     alpha, beta))
+
+
+def st_inplace_fma(strategy, config, a, b, c, basis, num_batches, alpha=1.0, beta=1.0) -> Error:
+    """include/rpp/operations/basic/st_inplace_fma.hpp:50-80: a = alpha*a + beta * b sh c."""
+    _check_batches(strategy, a, b, c)
+    lib = _lib.load()
+    return _status(lib.rpp_gb_st_inplace_fma(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
+                                             strategy.dtype_code(), _p(a), _p(b), _p(c), num_batches, alpha, beta))
+
+
+def st_adj_mul(strategy, config, out, op, arg, basis, num_batches) -> Error:
+    """include/rpp/operations/basic/st_adj_mul.hpp:46-69: the adjoint of x -> op sh x."""
+    _check_batches(strategy, out, op, arg)
+    lib = _lib.load()
+    return _status(lib.rpp_gb_st_adj_mul(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
+                                         strategy.dtype_code(), _p(out), _p(op), _p(arg), num_batches))
+
+
+def left_hs_mul(strategy, config, out, integrator, integrand, basis, num_batches, beta=1.0) -> Error:
+    """include/rpp/operations/basic/left_hs_mul.hpp:59-87: out = beta * integrator < integrand."""
+    _check_batches(strategy, out, integrator, integrand)
+    lib = _lib.load()
+    return _status(lib.rpp_gb_left_hs_mul(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
+                                          strategy.dtype_code(), _p(out), _p(integrator), _p(integrand),
+                                          num_batches, beta))
+
+
+def left_hs_adj_lmul(strategy, config, out, op, arg, basis, num_batches, beta=1.0) -> Error:
+    """include/rpp/operations/basic/left_hs_adj_lmul.hpp:39-57: adjoint of
+    y -> op < y (op = the fixed integrator, arg = the cotangent)."""
+    _check_batches(strategy, out, op, arg)
+    lib = _lib.load()
+    return _status(lib.rpp_gb_left_hs_adj_lmul(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
+                                               strategy.dtype_code(), _p(out), _p(op), _p(arg), num_batches, beta))
+
+
+def left_hs_adj_rmul(strategy, config, out, op, arg, basis, num_batches, beta=1.0) -> Error:
+    """include/rpp/operations/basic/left_hs_adj_rmul.hpp:39-57: adjoint of
+    x -> x < arg (op = the cotangent, arg = the fixed integrand)."""
+    _check_batches(strategy, out, op, arg)
+    lib = _lib.load()
+    return _status(lib.rpp_gb_left_hs_adj_rmul(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
+                                               strategy.dtype_code(), _p(out), _p(op), _p(arg), num_batches, beta))
+
+
+class ScalarBatch:
+    """rpp::make_scalar_batch (include/rpp/views/scalar_view.hpp:53-60): one
+    scalar per batch element, contiguous."""
+
+    def __init__(self, data):
+        self.data = data
+
+
+def make_scalar_batch(data) -> ScalarBatch:
+    return ScalarBatch(data)
+
+
+def tensor_pairing(strategy, config, result, functional, arg, basis, num_batches) -> Error:
+    """include/rpp/operations/basic/tensor_pairing.hpp:47-73: result[b] =
+    <functional_b, arg_b> over the degrees both views hold."""
+    _check_batches(strategy, result, functional, arg)
+    t = result.data
+    if t.dim() != 1 or not t.is_contiguous() or t.numel() < num_batches:
+        raise ValueError("tensor_pairing: result must be a contiguous 1-D tensor of num_batches scalars")
+    lib = _lib.load()
+    return _status(lib.rpp_gb_tensor_pairing(basis.plan(strategy.device), _cfg(config).handle(strategy.device),
+                                             strategy.dtype_code(), t.data_ptr(), _p(functional), _p(arg),
+                                             num_batches))
 
 
 def tensor_generalised_antipode(policy, strategy, config, out, arg, basis, num_batches) -> Error:

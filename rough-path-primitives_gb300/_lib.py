@@ -62,6 +62,14 @@ SIGNATURES = {
     "rpp_gb_ft_adj_lmul": [_vp, _vp, _i32, _P, _P, _P, _i64],
     "rpp_gb_ft_adj_rmul": [_vp, _vp, _i32, _P, _P, _P, _i64],
     "rpp_gb_tensor_antipode": [_vp, _vp, _i32, _i32, _P, _P, _i64],
+    "rpp_gb_st_mul": [_vp, _vp, _i32, _P, _P, _P, _i64, _dbl],
+    "rpp_gb_st_fma": [_vp, _vp, _i32, _P, _P, _P, _P, _i64, _dbl, _dbl],
+    "rpp_gb_st_inplace_fma": [_vp, _vp, _i32, _P, _P, _P, _i64, _dbl, _dbl],
+    "rpp_gb_st_adj_mul": [_vp, _vp, _i32, _P, _P, _P, _i64],
+    "rpp_gb_left_hs_mul": [_vp, _vp, _i32, _P, _P, _P, _i64, _dbl],
+    "rpp_gb_left_hs_adj_lmul": [_vp, _vp, _i32, _P, _P, _P, _i64, _dbl],
+    "rpp_gb_left_hs_adj_rmul": [_vp, _vp, _i32, _P, _P, _P, _i64, _dbl],
+    "rpp_gb_tensor_pairing": [_vp, _vp, _i32, _vp, _P, _P, _i64],
     "rpp_gb_vector_assign": [_vp, _vp, _i32, _P, _P, _i64],
     "rpp_gb_vector_set_constant": [_vp, _vp, _i32, _P, _i64, _dbl],
     "rpp_gb_tensor_set_identity": [_vp, _vp, _i32, _P, _i64, _dbl],

@@ -385,6 +385,80 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
 
 }  // namespace
 
+// Shuffle algebra: operand conversion and order computation shared by the
+// entry points below.
+template <typename T>
+int run_shuffle_product(const rpp_gb_plan* plan, cudaStream_t s, rpp_gb::ShuffleKind kind,
+                        const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* add, const rpp_gb_tensor_arg* lhs,
+                        const rpp_gb_tensor_arg* rhs, int64_t batch, double alpha, double beta) {
+    rpp_gb::TArg<T> o, a, l, r;
+    const auto& g = plan->geometry;
+    const bool left_half = kind == rpp_gb::ShuffleKind::LeftHalf;
+    if (!to_targ(out, g, true, batch, o, kind == rpp_gb::ShuffleKind::InplaceFma ? "a" : "out", true) ||
+        !to_targ(add, g, false, batch, a, "a") || !to_targ(lhs, g, true, batch, l, left_half ? "integrator" : "lhs") ||
+        !to_targ(rhs, g, true, batch, r, left_half ? "integrand" : "rhs"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    const auto ord = rpp_gb::shuffle_product_order(g, o.lo, o.hi);
+    return cuda_status(
+        rpp_gb::launch_shuffle_product<T>(g, plan->device, s, kind, o, a, l, r, batch, alpha, beta, ord),
+        "shuffle product kernel");
+}
+
+int run_shuffle_product_any(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, rpp_gb::ShuffleKind kind,
+                            const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* add,
+                            const rpp_gb_tensor_arg* lhs, const rpp_gb_tensor_arg* rhs, int64_t batch, double alpha,
+                            double beta) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64
+                   ? run_shuffle_product<double>(plan, s, kind, out, add, lhs, rhs, batch, alpha, beta)
+                   : run_shuffle_product<float>(plan, s, kind, out, add, lhs, rhs, batch, alpha, beta);
+    });
+}
+
+template <typename T>
+int run_shuffle_adjoint(const rpp_gb_plan* plan, cudaStream_t s, rpp_gb::ShuffleAdjKind kind,
+                        const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op, const rpp_gb_tensor_arg* arg,
+                        int64_t batch, double beta) {
+    rpp_gb::TArg<T> o, p, a;
+    const auto& g = plan->geometry;
+    if (!to_targ(out, g, true, batch, o, "out", true) || !to_targ(op, g, true, batch, p, "op") ||
+        !to_targ(arg, g, true, batch, a, "arg"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    // the kernels read the fixed operand through `op` and the cotangent
+    // through `arg`: the right adjoint's fixed operand is the integrand
+    const bool swap = kind == rpp_gb::ShuffleAdjKind::HalfR;
+    const auto& fixed = swap ? a : p;
+    const auto& cot = swap ? p : a;
+    const auto ord = rpp_gb::shuffle_adjoint_order(g, kind, o.lo, o.hi, fixed.lo, fixed.hi, cot.lo, cot.hi);
+    return cuda_status(
+        rpp_gb::launch_shuffle_adjoint<T>(g, plan->device, s, kind, o, fixed, cot, batch, beta, ord),
+        "shuffle adjoint kernel");
+}
+
+int run_shuffle_adjoint_any(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                            rpp_gb::ShuffleAdjKind kind, const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op,
+                            const rpp_gb_tensor_arg* arg, int64_t batch, double beta) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_shuffle_adjoint<double>(plan, s, kind, out, op, arg, batch, beta)
+                                   : run_shuffle_adjoint<float>(plan, s, kind, out, op, arg, batch, beta);
+    });
+}
+
+template <typename T>
+int run_pairing(const rpp_gb_plan* plan, cudaStream_t s, void* result, const rpp_gb_tensor_arg* f,
+                const rpp_gb_tensor_arg* a, int64_t batch) {
+    rpp_gb::TArg<T> tf, ta;
+    const auto& g = plan->geometry;
+    if (!result) return fail(RPP_GB_INVALID_ARGUMENT, "tensor_pairing: result is NULL");
+    if (!to_targ(f, g, true, batch, tf, "functional") || !to_targ(a, g, true, batch, ta, "arg"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    return cuda_status(rpp_gb::launch_pairing<T>(g, plan->device, s, static_cast<T*>(result), tf, ta, batch),
+                       "pairing kernel");
+}
+
+
 extern "C" {
 
 const char* rpp_gb_last_error_string(void) { return g_last_error.c_str(); }
@@ -498,6 +572,58 @@ int rpp_gb_ft_adj_rmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dt
         auto s = static_cast<cudaStream_t>(stream);
         return dtype == RPP_GB_F64 ? run_adjoint<double>(plan, s, false, out, op, arg, batch)
                                    : run_adjoint<float>(plan, s, false, out, op, arg, batch);
+    });
+}
+
+int rpp_gb_st_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                  const rpp_gb_tensor_arg* lhs, const rpp_gb_tensor_arg* rhs, int64_t batch, double beta) {
+    return run_shuffle_product_any(plan, stream, dtype, rpp_gb::ShuffleKind::Mul, out, nullptr, lhs, rhs, batch, 0.0,
+                                   beta);
+}
+
+int rpp_gb_st_fma(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                  const rpp_gb_tensor_arg* a, const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c, int64_t batch,
+                  double alpha, double beta) {
+    return run_shuffle_product_any(plan, stream, dtype, rpp_gb::ShuffleKind::Fma, out, a, b, c, batch, alpha, beta);
+}
+
+int rpp_gb_st_inplace_fma(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* a,
+                          const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c, int64_t batch, double alpha,
+                          double beta) {
+    return run_shuffle_product_any(plan, stream, dtype, rpp_gb::ShuffleKind::InplaceFma, a, nullptr, b, c, batch,
+                                   alpha, beta);
+}
+
+int rpp_gb_st_adj_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                      const rpp_gb_tensor_arg* op, const rpp_gb_tensor_arg* arg, int64_t batch) {
+    return run_shuffle_adjoint_any(plan, stream, dtype, rpp_gb::ShuffleAdjKind::Shuffle, out, op, arg, batch, 1.0);
+}
+
+int rpp_gb_left_hs_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,
+                       const rpp_gb_tensor_arg* integrator, const rpp_gb_tensor_arg* integrand, int64_t batch,
+                       double beta) {
+    return run_shuffle_product_any(plan, stream, dtype, rpp_gb::ShuffleKind::LeftHalf, out, nullptr, integrator,
+                                   integrand, batch, 0.0, beta);
+}
+
+int rpp_gb_left_hs_adj_lmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                            const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op, const rpp_gb_tensor_arg* arg,
+                            int64_t batch, double beta) {
+    return run_shuffle_adjoint_any(plan, stream, dtype, rpp_gb::ShuffleAdjKind::HalfL, out, op, arg, batch, beta);
+}
+
+int rpp_gb_left_hs_adj_rmul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                            const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* op, const rpp_gb_tensor_arg* arg,
+                            int64_t batch, double beta) {
+    return run_shuffle_adjoint_any(plan, stream, dtype, rpp_gb::ShuffleAdjKind::HalfR, out, op, arg, batch, beta);
+}
+
+int rpp_gb_tensor_pairing(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, void* result,
+                          const rpp_gb_tensor_arg* functional, const rpp_gb_tensor_arg* arg, int64_t batch) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_pairing<double>(plan, s, result, functional, arg, batch)
+                                   : run_pairing<float>(plan, s, result, functional, arg, batch);
     });
 }
 

@@ -72,6 +72,48 @@ cudaError_t launch_spmm(const CsrDevice& m, const DeviceInfo& dev, cudaStream_t 
                         int64_t out_stride, int64_t out_size, const T* arg, int64_t arg_stride,
                         int64_t arg_size, int64_t batch, double alpha);
 
+// Shuffle algebra (shuffle.cu).
+enum class ShuffleKind : int {
+    Mul = 0,         // out = beta * lhs sh rhs
+    Fma = 1,         // out = alpha*add + beta * lhs sh rhs   (add may be absent)
+    InplaceFma = 2,  // out = alpha*out + beta * lhs sh rhs
+    LeftHalf = 3,    // out = beta * lhs < rhs, out[0] = 0
+};
+
+enum class ShuffleAdjKind : int {
+    Shuffle = 0,  // st_adj_mul(out, op, arg)
+    HalfL = 1,    // left_hs_adj_lmul: op = integrator, arg = integrand
+    HalfR = 2,    // left_hs_adj_rmul: op = integrand, arg = integrator
+};
+
+// Order in which a shuffle kernel visits the output degrees: entry e covers
+// degree deg[e], output positions [start[e], start[e+1]); the first
+// warp_entries entries give each coefficient a warp.
+struct ShuffleOrder {
+    int count;
+    int warp_entries;
+    int deg[kMaxDepth + 1];
+    uint32_t start[kMaxDepth + 2];
+};
+
+ShuffleOrder shuffle_product_order(const Geometry& g, int out_lo, int out_hi);
+ShuffleOrder shuffle_adjoint_order(const Geometry& g, ShuffleAdjKind kind, int out_lo, int out_hi, int op_lo,
+                                   int op_hi, int arg_lo, int arg_hi);
+
+template <typename T>
+cudaError_t launch_shuffle_product(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ShuffleKind kind,
+                                   TArg<T> out, TArg<T> add, TArg<T> lhs, TArg<T> rhs, int64_t batch, double alpha,
+                                   double beta, const ShuffleOrder& ord);
+
+template <typename T>
+cudaError_t launch_shuffle_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ShuffleAdjKind kind,
+                                   TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch, double beta,
+                                   const ShuffleOrder& ord);
+
+template <typename T>
+cudaError_t launch_pairing(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, T* result, TArg<T> f, TArg<T> a,
+                           int64_t batch);
+
 // Fused signature kernels.
 struct PathBatch {
     const int64_t* offsets;  // device, batch + 1 (or nullptr)

@@ -1,0 +1,534 @@
+// shuffle.cu -- the shuffle algebra on batches of tensors (sm_103a).
+//
+// Products (include/rpp/operations/basic/st_mul.hpp, st_fma.hpp,
+// st_inplace_fma.hpp, left_hs_mul.hpp; coefficient definition in
+// include/rpp/operations/implementation/word_shuffle_product.hpp:43-97 and
+// word_half_shuffle_product.hpp:12-56):
+//   (L sh R)[w]     = sum over position subsets S of w of L[w|S] R[w|S^c]
+//   (L < R)[a v]    = sum over subsets S of v of L[a (v|S)] R[v|S^c]
+// Adjoints (st_adj_mul.hpp, left_hs_adj_lmul.hpp, left_hs_adj_rmul.hpp; the
+// interleaving sums of operations/implementation/shuffle_adjoint_op_loop.hpp
+// and word_shuffle_adjoint_multiply.hpp):
+//   st_adj_mul  out[w]   = sum_u op[u] sum_{s in w sh u} arg[s]
+//   hs_adj_lmul out[w]   = beta sum_a sum_u X[a u] sum_{s in w sh u} Y[a s]
+//   hs_adj_rmul out[a v] = beta sum_u Y[u] sum_{s in v sh u} X[a s], out[0] = 0
+// (X = integrator, Y = integrand, in the reference operator's argument order).
+// tensor_pairing (tensor_pairing.hpp) is the batched dot product over the
+// degrees both views hold.
+//
+// Every FP64 coefficient costs one FMA per (subset) term and the integer work
+// that locates the two factors is kept under ~10 instructions per FMA, so the
+// kernels are bound by the FP64 pipe.  Each CTA owns one tensor of the batch
+// at a time (grid-stride), stages the two operands in shared memory when they
+// fit and writes every output coefficient exactly once: results are
+// deterministic and no atomics are used.
+//
+// Work order: output degrees are visited in the order the host computes
+// (most expensive per coefficient first).  Degrees whose coefficients are
+// expensive (the low degrees of the adjoints) give each coefficient a warp;
+// the rest give each coefficient one thread, 32 consecutive coefficients per
+// task.  Warps take tasks from a shared-memory counter.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "launch_util.cuh"
+#include "ops.hpp"
+
+namespace rpp_gb {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T warp_reduce(T v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ void stage_range(T* dst, const T* src, int lo, int hi, const Geometry& G) {
+    if (lo > hi) return;
+    const uint32_t b = G.db[lo], e = G.db[hi + 1];
+    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) dst[i] = src[i];
+}
+
+// Output position k of the visiting order -> (degree, index in degree).
+__device__ __forceinline__ void locate(const ShuffleOrder& ord, uint32_t k, int& n, uint32_t& j) {
+    int e = 0;
+    while (e + 1 < ord.count && ord.start[e + 1] <= k) ++e;
+    n = ord.deg[e];
+    j = k - ord.start[e];
+}
+
+// ---------------------------------------------------------------------------
+// Forward products.
+// ---------------------------------------------------------------------------
+
+// sum over subsets S of the m letters of v of Lget(|S|)[v|S] * R[|S^c|][v|S^c]
+// where Lget(k) reads level k + e at offset a W^k (e = 1: the integrator of a
+// half-shuffle with prefix letter a).  Mask bit t selects letter t counted from
+// the last, as in the reference's masked packing; masks are visited in
+// increasing order (high part outer, 3 low bits inner), which is the
+// reference's summation order.
+template <typename T, int MAXD>
+__device__ T shuffle_word(const Geometry& G, int m, uint32_t v, int e, uint32_t a, const T* __restrict__ L,
+                          int llo, int lhi, const T* __restrict__ R, int rlo, int rhi) {
+    const uint32_t W = static_cast<uint32_t>(G.width);
+    uint32_t d[MAXD];
+    {
+        uint32_t x = v;
+#pragma unroll
+        for (int t = 0; t < MAXD; ++t) {
+            if (t < m) {
+                uint32_t q, r;
+                G.divw.divmod(x, q, r);
+                d[t] = r;
+                x = q;
+            }
+        }
+    }
+    const int h = m < 3 ? m : 3;
+    const int nlow = 1 << h;
+    // low tables: the last h letters split by each low mask
+    uint32_t lowL[8], lowR[8];
+#pragma unroll
+    for (int lm = 0; lm < 8; ++lm) {
+        uint32_t l = 0, r = 0;
+#pragma unroll
+        for (int t = 2; t >= 0; --t) {
+            if (t < h) {
+                if ((lm >> t) & 1) l = l * W + d[t];
+                else r = r * W + d[t];
+            }
+        }
+        lowL[lm] = l;
+        lowR[lm] = r;
+    }
+    // W^c for the c low letters taken left, W^(h-c) for the h-c taken right
+    uint32_t pwl[4], pwr[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        pwl[c] = G.pw[c];
+        pwr[c] = c <= h ? G.pw[h - c] : 0u;
+    }
+
+    T acc = T(0);
+    const uint32_t nhigh = 1u << (m - h);
+    for (uint32_t hm = 0; hm < nhigh; ++hm) {
+        uint32_t hl = 0, hr = 0;
+        int kh = 0;
+#pragma unroll
+        for (int t = MAXD - 1; t >= 3; --t) {
+            if (t < m) {
+                if ((hm >> (t - h)) & 1u) {
+                    hl = hl * W + d[t];
+                    ++kh;
+                } else {
+                    hr = hr * W + d[t];
+                }
+            }
+        }
+        // per number c of low letters taken left: bases and validity
+        uint32_t lb[4], rb[4];
+        bool ok[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int kl = kh + c, kr = m - kl;
+            ok[c] = c <= h && kr >= 0 && kl + e >= llo && kl + e <= lhi && kr >= rlo && kr <= rhi;
+            lb[c] = ok[c] ? G.db[kl + e] + a * G.pw[kl] + hl * pwl[c] : 0u;
+            rb[c] = ok[c] ? G.db[kr] + hr * pwr[c] : 0u;
+        }
+#pragma unroll
+        for (int lm = 0; lm < 8; ++lm) {
+            const int c = __builtin_popcount(lm);
+            if (lm < nlow && ok[c]) acc = fma(L[lb[c] + lowL[lm]], R[rb[c] + lowR[lm]], acc);
+        }
+    }
+    return acc;
+}
+
+template <typename T, int MAXD>
+__global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, TArg<T> out, TArg<T> add, TArg<T> lhs,
+                                                        TArg<T> rhs, int64_t batch, T alpha, T beta, int staged,
+                                                        ShuffleOrder ord) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    __shared__ uint32_t s_next;
+    const int e = kind == static_cast<int>(ShuffleKind::LeftHalf) ? 1 : 0;
+    const int lhi = imin(lhs.hi, G.depth), rhi = imin(rhs.hi, G.depth);
+    const uint32_t total = ord.start[ord.count];
+    const uint32_t ntasks = (total + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        const T* L = lhs.at(b);
+        const T* R = rhs.at(b);
+        T* o = out.at(b);
+        const T* A = add.p ? add.at(b) : nullptr;
+        if (threadIdx.x == 0) s_next = 0;
+        if (staged) {
+            stage_range(sm, L, lhs.lo, lhi, G);
+            stage_range(sm + G.dim, R, rhs.lo, rhi, G);
+            L = sm;
+            R = sm + G.dim;
+        }
+        __syncthreads();
+        for (;;) {
+            uint32_t t = 0;
+            if (lane == 0) t = atomicAdd(&s_next, 1u);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            if (t >= ntasks) break;
+            const uint32_t k = t * 32 + lane;
+            if (k < total) {
+                int n;
+                uint32_t j;
+                locate(ord, k, n, j);
+                T val;
+                if (e) {
+                    if (n == 0) {
+                        val = T(0);
+                    } else {
+                        const uint32_t tail = G.pw[n - 1];
+                        const uint32_t a = j / tail, v = j - a * tail;
+                        val = beta * shuffle_word<T, MAXD>(G, n - 1, v, 1, a, L, lhs.lo, lhi, R, rhs.lo, rhi);
+                    }
+                } else {
+                    val = beta * shuffle_word<T, MAXD>(G, n, j, 0, 0u, L, lhs.lo, lhi, R, rhs.lo, rhi);
+                    if (kind == static_cast<int>(ShuffleKind::InplaceFma)) {
+                        val = fma(alpha, o[G.db[n] + j], val);
+                    } else if (kind == static_cast<int>(ShuffleKind::Fma) && A && add.has(n)) {
+                        val = fma(alpha, A[G.db[n] + j], val);
+                    }
+                }
+                o[G.db[n] + j] = val;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoints.
+// ---------------------------------------------------------------------------
+
+// Interleaving sum for one output word w (nw letters) and one op degree m:
+//   sum_u OP[ob + u] * ARG[ab + merge(w, u, M)] over the masks M of weight m
+// on nw + m positions (bit b = position b counted from the last letter) and
+// the op words u.  u is split as u_hi W + u_0: a walk over the positions
+// places w's and u_hi's letters, then the inner loop runs over u_0, whose
+// position is the lowest set bit of M.  Lanes [lane0, lane0 + lanes) of a warp
+// share the u_hi range (lanes = 1 for a single thread).
+template <typename T>
+__device__ T interleave_sum(const Geometry& G, int nw, uint32_t w, int m, const T* __restrict__ OP, uint32_t ob,
+                            const T* __restrict__ ARG, uint32_t ab, uint32_t first, uint32_t step) {
+    const uint32_t W = static_cast<uint32_t>(G.width);
+    if (m == 0) return first == 0 ? OP[ob] * ARG[ab + w] : T(0);
+    const int N = nw + m;
+    const uint32_t nhi = G.pw[m - 1];
+    T acc = T(0);
+    uint32_t M = (1u << m) - 1u;
+    const uint32_t last = M << nw;
+    for (;;) {
+        const uint32_t low = M & (0u - M);
+        const uint32_t rest = M & (M - 1u);
+        const uint32_t c0 = G.pw[__ffs(M) - 1];
+        for (uint32_t uh = first; uh < nhi; uh += step) {
+            uint32_t wq = w, uq = uh, base = 0, p = 1;
+            for (int bpos = 0; bpos < N; ++bpos) {
+                const uint32_t bit = 1u << bpos;
+                if (!(low & bit)) {
+                    const bool from_u = (rest & bit) != 0;
+                    const uint32_t src = from_u ? uq : wq;
+                    uint32_t q, r;
+                    G.divw.divmod(src, q, r);
+                    if (from_u) uq = q;
+                    else wq = q;
+                    base += r * p;
+                }
+                p *= W;
+            }
+            const T* op = OP + ob + uh * W;
+            const T* ar = ARG + ab + base;
+            for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
+        }
+        if (M == last) break;
+        // next mask of the same weight (Gosper)
+        const uint32_t ripple = M + low;
+        M = ripple | (((ripple ^ M) >> 2) >> (__ffs(M) - 1));
+    }
+    return acc;
+}
+
+struct AdjRange {
+    int lo, hi;
+};
+
+// The op-degree range of one output degree n (reference bounds, see the
+// per-kind comments in the file header).
+__device__ __forceinline__ AdjRange adj_range(int kind, int n, int olo, int ohi, int alo, int ahi) {
+    if (kind == static_cast<int>(ShuffleAdjKind::HalfL))
+        return {imax(0, imax(olo - 1, alo - 1 - n)), imin(ohi - 1, ahi - 1 - n)};
+    return {imax(olo, alo - n), imin(ohi, ahi - n)};
+}
+
+template <typename T>
+__device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const T* OP, int olo, int ohi,
+                           const T* ARG, int alo, int ahi, uint32_t first, uint32_t step) {
+    const AdjRange r = adj_range(kind, n, olo, ohi, alo, ahi);
+    T acc = T(0);
+    if (kind == static_cast<int>(ShuffleAdjKind::Shuffle)) {
+        for (int m = r.lo; m <= r.hi; ++m)
+            acc += interleave_sum<T>(G, n, j, m, OP, G.db[m], ARG, G.db[n + m], first, step);
+    } else if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
+        const uint32_t W = static_cast<uint32_t>(G.width);
+        for (int m = r.lo; m <= r.hi; ++m) {
+            // lanes split (letter, u_hi); a thread (step 1) loops over both
+            const uint32_t nhi = m == 0 ? 1u : G.pw[m - 1];
+            for (uint32_t a = 0; a < W; ++a) {
+                // lane slice of this letter's u_hi range in the combined space
+                const uint32_t lo = a * nhi, hi = lo + nhi;
+                uint32_t f = first;
+                if (step > 1) {
+                    if (f < lo) f += ((lo - f + step - 1) / step) * step;
+                    if (f >= hi) continue;
+                } else {
+                    f = lo + first;
+                }
+                acc += interleave_sum<T>(G, n, j, m, OP, G.db[m + 1] + a * G.pw[m], ARG,
+                                         G.db[n + m + 1] + a * G.pw[n + m], f - lo, step);
+            }
+        }
+    } else {
+        if (n == 0) return T(0);
+        const uint32_t tail = G.pw[n - 1];
+        const uint32_t a = j / tail, v = j - a * tail;
+        for (int m = r.lo; m <= r.hi; ++m)
+            acc += interleave_sum<T>(G, n - 1, v, m, OP, G.db[m], ARG, G.db[n + m] + a * G.pw[n - 1 + m], first,
+                                     step);
+    }
+    return acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, TArg<T> out, TArg<T> op,
+                                                        TArg<T> arg, int64_t batch, T beta, int staged,
+                                                        ShuffleOrder ord) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    __shared__ uint32_t s_next;
+    const int ohi = imin(op.hi, G.depth), ahi = imin(arg.hi, G.depth);
+    const uint32_t nwarp = ord.start[ord.warp_entries];
+    const uint32_t total = ord.start[ord.count];
+    const uint32_t ntasks = nwarp + (total - nwarp + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        const T* P = op.at(b);
+        const T* A = arg.at(b);
+        T* o = out.at(b);
+        if (threadIdx.x == 0) s_next = 0;
+        if (staged) {
+            stage_range(sm, P, op.lo, ohi, G);
+            stage_range(sm + G.dim, A, arg.lo, ahi, G);
+            P = sm;
+            A = sm + G.dim;
+        }
+        __syncthreads();
+        for (;;) {
+            uint32_t t = 0;
+            if (lane == 0) t = atomicAdd(&s_next, 1u);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            if (t >= ntasks) break;
+            if (t < nwarp) {
+                int n;
+                uint32_t j;
+                locate(ord, t, n, j);
+                T acc = adjoint_coeff<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi, lane, 32);
+                acc = warp_reduce(acc);
+                if (lane == 0) o[G.db[n] + j] = beta * acc;
+            } else {
+                const uint32_t k = nwarp + (t - nwarp) * 32 + lane;
+                if (k < total) {
+                    int n;
+                    uint32_t j;
+                    locate(ord, k, n, j);
+                    const T acc = adjoint_coeff<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi, 0, 1);
+                    o[G.db[n] + j] = beta * acc;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// tensor_pairing: one warp per tensor of the batch.
+template <typename T>
+__global__ void k_pairing(const T* __restrict__ F, int64_t fs, const T* __restrict__ A, int64_t as, T* result,
+                          uint32_t begin, uint32_t end, int64_t batch) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+    for (int64_t b = blockIdx.x * static_cast<int64_t>(blockDim.x >> 5) + (threadIdx.x >> 5); b < batch;
+         b += warps) {
+        const T* f = F + b * fs;
+        const T* a = A + b * as;
+        T acc = T(0);
+        for (uint32_t i = begin + lane; i < end; i += 32) acc = fma(f[i], a[i], acc);
+        acc = warp_reduce(acc);
+        if (lane == 0) result[b] = acc;
+    }
+}
+
+constexpr size_t kStageLimit = 200 * 1024;
+
+template <typename Kernel>
+cudaError_t shuffle_launch_shape(Kernel kernel, const Geometry& g, const DeviceInfo& dev, size_t elem, int64_t batch,
+                                 int& threads, size_t& smem, int& staged, dim3& grid) {
+    const size_t need = 2 * static_cast<size_t>(g.dim) * elem;
+    staged = need <= kStageLimit && need <= static_cast<size_t>(dev.max_smem_optin) ? 1 : 0;
+    smem = staged ? need : 0;
+    threads = threads_for(g.pw[g.depth]);
+    if (threads < 64) threads = 64;
+    return batch_grid(kernel, dev, threads, smem, batch, grid);
+}
+
+}  // namespace
+
+ShuffleOrder shuffle_product_order(const Geometry& g, int out_lo, int out_hi) {
+    // a coefficient of degree n costs 2^n terms: visit the top degree first
+    ShuffleOrder o{};
+    const int hi = out_hi < g.depth ? out_hi : g.depth;
+    uint32_t acc = 0;
+    for (int n = hi; n >= out_lo && n >= 0; --n) {
+        o.deg[o.count] = n;
+        o.start[o.count] = acc;
+        acc += g.pw[n];
+        ++o.count;
+    }
+    o.start[o.count] = acc;
+    return o;
+}
+
+ShuffleOrder shuffle_adjoint_order(const Geometry& g, ShuffleAdjKind kind, int out_lo, int out_hi, int op_lo,
+                                   int op_hi, int arg_lo, int arg_hi) {
+    // Terms per coefficient of degree n: sum over op degrees m of
+    // C(nw + m, m) W^m (times W for the left adjoint's letter loop).
+    // Coefficients of at least kWarpTerms terms get a warp each.
+    constexpr double kWarpTerms = 1024.0;
+    struct Entry {
+        int n;
+        double cost;
+    };
+    Entry e[kMaxDepth + 1];
+    int count = 0;
+    const int D = g.depth;
+    const int ohi = op_hi < D ? op_hi : D, ahi = arg_hi < D ? arg_hi : D;
+    const double W = static_cast<double>(g.width);
+    for (int n = out_lo < 0 ? 0 : out_lo; n <= out_hi && n <= D; ++n) {
+        int lo, hi, nw = n;
+        if (kind == ShuffleAdjKind::HalfL) {
+            lo = std::max({0, op_lo - 1, arg_lo - 1 - n});
+            hi = std::min(ohi - 1, ahi - 1 - n);
+        } else {
+            lo = std::max(op_lo, arg_lo - n);
+            hi = std::min(ohi, ahi - n);
+            if (kind == ShuffleAdjKind::HalfR) nw = n - 1;
+        }
+        double cost = 0.0;
+        if (!(kind == ShuffleAdjKind::HalfR && n == 0)) {
+            for (int m = lo < 0 ? 0 : lo; m <= hi; ++m) {
+                double c = 1.0;  // C(nw + m, m)
+                for (int i = 1; i <= m; ++i) c = c * (nw + i) / i;
+                cost += c * std::pow(W, m);
+            }
+            if (kind == ShuffleAdjKind::HalfL) cost *= W;
+        }
+        e[count++] = {n, cost};
+    }
+    std::stable_sort(e, e + count, [](const Entry& x, const Entry& y) { return x.cost > y.cost; });
+    ShuffleOrder o{};
+    uint32_t acc = 0;
+    for (int i = 0; i < count; ++i) {
+        o.deg[i] = e[i].n;
+        o.start[i] = acc;
+        acc += g.pw[e[i].n];
+        if (e[i].cost >= kWarpTerms && o.warp_entries == i) o.warp_entries = i + 1;
+    }
+    o.count = count;
+    o.start[count] = acc;
+    return o;
+}
+
+template <typename T>
+cudaError_t launch_shuffle_product(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ShuffleKind kind,
+                                   TArg<T> out, TArg<T> add, TArg<T> lhs, TArg<T> rhs, int64_t batch, double alpha,
+                                   double beta, const ShuffleOrder& ord) {
+    if (batch <= 0 || ord.start[ord.count] == 0) return cudaSuccess;
+    if (g.depth > 30) return cudaErrorInvalidValue;
+    int threads, staged;
+    size_t smem;
+    dim3 grid;
+    cudaError_t err;
+#define RPP_GB_SHUFFLE_FWD(MAXD)                                                                           \
+    {                                                                                                      \
+        constexpr auto kernel = k_shuffle_product<T, MAXD>;                                                \
+        if ((err = allow_large_smem<kernel>(dev)) != cudaSuccess) return err;                              \
+        if ((err = shuffle_launch_shape(kernel, g, dev, sizeof(T), batch, threads, smem, staged, grid)) != \
+            cudaSuccess)                                                                                   \
+            return err;                                                                                    \
+        kernel<<<grid, threads, smem, s>>>(g, static_cast<int>(kind), out, add, lhs, rhs, batch,           \
+                                           static_cast<T>(alpha), static_cast<T>(beta), staged, ord);      \
+    }
+    if (g.depth <= 8) RPP_GB_SHUFFLE_FWD(8)
+    else if (g.depth <= 16) RPP_GB_SHUFFLE_FWD(16)
+    else RPP_GB_SHUFFLE_FWD(32)
+#undef RPP_GB_SHUFFLE_FWD
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_shuffle_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ShuffleAdjKind kind,
+                                   TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch, double beta,
+                                   const ShuffleOrder& ord) {
+    if (batch <= 0 || ord.start[ord.count] == 0) return cudaSuccess;
+    constexpr auto kernel = k_shuffle_adjoint<T>;
+    cudaError_t err = allow_large_smem<kernel>(dev);
+    if (err != cudaSuccess) return err;
+    int threads, staged;
+    size_t smem;
+    dim3 grid;
+    if ((err = shuffle_launch_shape(kernel, g, dev, sizeof(T), batch, threads, smem, staged, grid)) != cudaSuccess)
+        return err;
+    kernel<<<grid, threads, smem, s>>>(g, static_cast<int>(kind), out, op, arg, batch, static_cast<T>(beta), staged,
+                                       ord);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_pairing(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, T* result, TArg<T> f, TArg<T> a,
+                           int64_t batch) {
+    if (batch <= 0) return cudaSuccess;
+    const int lo = f.lo > a.lo ? f.lo : a.lo;
+    int hi = f.hi < a.hi ? f.hi : a.hi;
+    if (hi > g.depth) hi = g.depth;
+    const uint32_t begin = lo <= hi ? g.db[lo] : 0u, end = lo <= hi ? g.db[hi + 1] : 0u;
+    const int threads = 256;
+    const int64_t blocks_needed = (batch + 7) / 8;
+    const int64_t cap = static_cast<int64_t>(dev.sm_count) * 8;
+    const unsigned blocks = static_cast<unsigned>(blocks_needed < cap ? blocks_needed : cap);
+    k_pairing<T><<<blocks, threads, 0, s>>>(f.p, f.stride, a.p, a.stride, result, begin, end, batch);
+    return cudaGetLastError();
+}
+
+#define RPP_GB_INSTANTIATE_SHUFFLE(T)                                                                           \
+    template cudaError_t launch_shuffle_product<T>(const Geometry&, const DeviceInfo&, cudaStream_t, ShuffleKind, \
+                                                   TArg<T>, TArg<T>, TArg<T>, TArg<T>, int64_t, double, double,   \
+                                                   const ShuffleOrder&);                                          \
+    template cudaError_t launch_shuffle_adjoint<T>(const Geometry&, const DeviceInfo&, cudaStream_t,              \
+                                                   ShuffleAdjKind, TArg<T>, TArg<T>, TArg<T>, int64_t, double,    \
+                                                   const ShuffleOrder&);                                          \
+    template cudaError_t launch_pairing<T>(const Geometry&, const DeviceInfo&, cudaStream_t, T*, TArg<T>, TArg<T>, \
+                                           int64_t);
+
+RPP_GB_INSTANTIATE_SHUFFLE(float)
+RPP_GB_INSTANTIATE_SHUFFLE(double)
+
+}  // namespace rpp_gb

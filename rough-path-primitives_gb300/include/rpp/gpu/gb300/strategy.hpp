@@ -352,6 +352,85 @@ RPP_GB300_TERNARY_OP(FTAdjRMul, rpp_gb_ft_adj_rmul)
 // vector_assign (include/rpp/operations/linalg/vector_assign.hpp)
 RPP_GB300_BINARY_OP(VectorAssign, rpp_gb_vector_assign)
 
+// ---- shuffle algebra (include/rpp/operations/basic/st_*.hpp, left_hs_*.hpp) -
+#define RPP_GB300_SCALED_TERNARY_OP(NAME, CALL)                                                               \
+    RPP_GB300_OP_HEADER(NAME)                                                                                 \
+        template <typename Batches, typename Bases>                                                           \
+        static Error<char const*> gb300_launch(Strategy const& s, gpu::DeviceLaunchConfig const& cfg,         \
+                                               Batches&& b, Bases&& bases, Index n,                           \
+                                               Accum beta = Accum{1}) noexcept {                              \
+            namespace d = gb300_ops_detail;                                                                   \
+            rpp_gb_plan const* plan = nullptr;                                                                \
+            if (auto e = d::plan_of(s, d::tensor_basis(bases), plan); !e) return e;                           \
+            auto o = d::tensor_arg(std::get<0>(b), bases), x = d::tensor_arg(std::get<1>(b), bases),          \
+                 y = d::tensor_arg(std::get<2>(b), bases);                                                    \
+            return d::status(CALL(plan, cfg.stream, gpu::strategies::gb300_detail::dtype_code<Accum>(), &o,  \
+                                  &x, &y, static_cast<int64_t>(n), static_cast<double>(beta)));               \
+        }                                                                                                     \
+    };
+
+// st_mul(out, lhs, rhs, beta) (st_mul.hpp:53-79)
+RPP_GB300_SCALED_TERNARY_OP(STMul, rpp_gb_st_mul)
+// left_hs_mul(out, integrator, integrand, beta) (left_hs_mul.hpp:59-87)
+RPP_GB300_SCALED_TERNARY_OP(LeftHSMul, rpp_gb_left_hs_mul)
+// left_hs_adj_lmul / left_hs_adj_rmul(out, op, arg, beta) (left_hs_adj_lmul.hpp:39-57,
+// left_hs_adj_rmul.hpp:39-57)
+RPP_GB300_SCALED_TERNARY_OP(LeftHSAdjLMul, rpp_gb_left_hs_adj_lmul)
+RPP_GB300_SCALED_TERNARY_OP(LeftHSAdjRMul, rpp_gb_left_hs_adj_rmul)
+// st_adj_mul(out, op, arg) (st_adj_mul.hpp:46-69)
+RPP_GB300_TERNARY_OP(STAdjMul, rpp_gb_st_adj_mul)
+
+// ---- st_fma (st_fma.hpp:56-85) ----------------------------------------------
+RPP_GB300_OP_HEADER(STFma)
+    template <typename Batches, typename Bases>
+    static Error<char const*> gb300_launch(Strategy const& s, gpu::DeviceLaunchConfig const& cfg, Batches&& b,
+                                           Bases&& bases, Index n, Accum alpha = Accum{1},
+                                           Accum beta = Accum{1}) noexcept {
+        namespace d = gb300_ops_detail;
+        rpp_gb_plan const* plan = nullptr;
+        if (auto e = d::plan_of(s, d::tensor_basis(bases), plan); !e) return e;
+        auto o = d::tensor_arg(std::get<0>(b), bases), x = d::tensor_arg(std::get<1>(b), bases),
+             y = d::tensor_arg(std::get<2>(b), bases), z = d::tensor_arg(std::get<3>(b), bases);
+        return d::status(rpp_gb_st_fma(plan, cfg.stream, gpu::strategies::gb300_detail::dtype_code<Accum>(), &o, &x,
+                                       &y, &z, static_cast<int64_t>(n), static_cast<double>(alpha),
+                                       static_cast<double>(beta)));
+    }
+};
+
+// ---- st_inplace_fma (st_inplace_fma.hpp:50-80) ------------------------------
+RPP_GB300_OP_HEADER(STInplaceFma)
+    template <typename Batches, typename Bases>
+    static Error<char const*> gb300_launch(Strategy const& s, gpu::DeviceLaunchConfig const& cfg, Batches&& b,
+                                           Bases&& bases, Index n, Accum alpha = Accum{1},
+                                           Accum beta = Accum{1}) noexcept {
+        namespace d = gb300_ops_detail;
+        rpp_gb_plan const* plan = nullptr;
+        if (auto e = d::plan_of(s, d::tensor_basis(bases), plan); !e) return e;
+        auto a = d::tensor_arg(std::get<0>(b), bases), x = d::tensor_arg(std::get<1>(b), bases),
+             y = d::tensor_arg(std::get<2>(b), bases);
+        return d::status(rpp_gb_st_inplace_fma(plan, cfg.stream, gpu::strategies::gb300_detail::dtype_code<Accum>(),
+                                               &a, &x, &y, static_cast<int64_t>(n), static_cast<double>(alpha),
+                                               static_cast<double>(beta)));
+    }
+};
+
+// ---- tensor_pairing(result, functional, arg) (tensor_pairing.hpp:47-73) -----
+// `result` is a scalar batch (rpp::make_scalar_batch) over a device array.
+RPP_GB300_OP_HEADER(TensorPairing)
+    template <typename Batches, typename Bases>
+    static Error<char const*> gb300_launch(Strategy const& s, gpu::DeviceLaunchConfig const& cfg, Batches&& b,
+                                           Bases&& bases, Index n) noexcept {
+        namespace d = gb300_ops_detail;
+        rpp_gb_plan const* plan = nullptr;
+        if (auto e = d::plan_of(s, d::tensor_basis(bases), plan); !e) return e;
+        auto f = d::tensor_arg(std::get<1>(b), bases), x = d::tensor_arg(std::get<2>(b), bases);
+        void* result = const_cast<void*>(
+            static_cast<void const*>(gpu::strategies::gb300_detail::raw(std::get<0>(b).data())));
+        return d::status(rpp_gb_tensor_pairing(plan, cfg.stream, gpu::strategies::gb300_detail::dtype_code<Accum>(),
+                                               result, &f, &x, static_cast<int64_t>(n)));
+    }
+};
+
 // ---- tensor_generalised_antipode<policy> ---------------------------------
 template <typename Accum_, typename Architecture_, TensorAntipodeSigningPolicy Policy>
 class TensorGeneralisedAntipode<gpu::strategies::GB300Strategy<Accum_, Architecture_>, Policy>

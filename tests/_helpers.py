@@ -19,3 +19,10 @@ def rel_err(actual, expected):
 def assert_close(actual, expected, tol=TOL_F64, what=""):
     e = rel_err(actual, expected)
     assert np.isfinite(e) and e <= tol, f"{what}: relative error {e:.3e} > {tol:.1e}"
+
+
+def shuffle_cases(z, op):
+    """The cases of one operation in a golden file written as
+    `<op>/<i>/<field>` keys, in case order."""
+    keys = sorted({k.split("/")[1] for k in z.files if k.startswith(op + "/")}, key=int)
+    return [{k.split("/")[2]: z[k] for k in z.files if k.startswith(f"{op}/{i}/")} for i in keys]

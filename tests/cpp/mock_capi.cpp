@@ -67,6 +67,30 @@ UNARY(vector_assign)
 BINARY(ft_fmexp)
 BINARY(ft_adj_lmul)
 BINARY(ft_adj_rmul)
+BINARY(st_adj_mul)
+#define SCALED(NAME)                                                                                  \
+    int rpp_gb_##NAME(const rpp_gb_plan*, rpp_gb_stream, int32_t t, const rpp_gb_tensor_arg* o,     \
+                      const rpp_gb_tensor_arg* x, const rpp_gb_tensor_arg* y, int64_t n, double b) { \
+        head(#NAME, t, n); rec("out", o); rec("x", x); rec("y", y); tail(0, b); return 0;             \
+    }
+SCALED(st_mul)
+SCALED(left_hs_mul)
+SCALED(left_hs_adj_lmul)
+SCALED(left_hs_adj_rmul)
+int rpp_gb_st_fma(const rpp_gb_plan*, rpp_gb_stream, int32_t t, const rpp_gb_tensor_arg* o, const rpp_gb_tensor_arg* a,
+                  const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c, int64_t n, double al, double be) {
+    head("st_fma", t, n); rec("out", o); rec("a", a); rec("b", b); rec("c", c); tail(al, be); return 0;
+}
+int rpp_gb_st_inplace_fma(const rpp_gb_plan*, rpp_gb_stream, int32_t t, const rpp_gb_tensor_arg* a,
+                          const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c, int64_t n, double al, double be) {
+    head("st_inplace_fma", t, n); rec("a", a); rec("b", b); rec("c", c); tail(al, be); return 0;
+}
+int rpp_gb_tensor_pairing(const rpp_gb_plan*, rpp_gb_stream, int32_t t, void* result, const rpp_gb_tensor_arg* f,
+                          const rpp_gb_tensor_arg* a, int64_t n) {
+    head("tensor_pairing", t, n);
+    std::snprintf(g_buf, sizeof g_buf, " result=%s", result ? "set" : "null"); g_calls += g_buf;
+    rec("f", f); rec("arg", a); tail(0, 0); return 0;
+}
 int rpp_gb_tensor_antipode(const rpp_gb_plan*, rpp_gb_stream, int32_t t, int32_t policy, const rpp_gb_tensor_arg* o,
                            const rpp_gb_tensor_arg* a, int64_t n) {
     head("tensor_antipode", t, n);

@@ -42,6 +42,15 @@ int main() {
     bad += !rpp::ops::ft_adj_rmul(s, cfg, part, full, one, basis, 4);
     bad += !rpp::ops::tensor_antipode(s, cfg, full, part, basis, 4);
     bad += !rpp::ops::tensor_reflect(s, cfg, full, part, basis, 4);
+    bad += !rpp::ops::st_mul(s, cfg, full, part, one, basis, 4, 0.5);
+    bad += !rpp::ops::st_fma(s, cfg, full, part, full, one, basis, 4, 0.25, 2.0);
+    bad += !rpp::ops::st_inplace_fma(s, cfg, full, one, part, basis, 4, 1.0, 0.5);
+    bad += !rpp::ops::st_adj_mul(s, cfg, part, full, one, basis, 4);
+    bad += !rpp::ops::left_hs_mul(s, cfg, full, part, one, basis, 4, 3.0);
+    bad += !rpp::ops::left_hs_adj_lmul(s, cfg, part, full, one, basis, 4);
+    bad += !rpp::ops::left_hs_adj_rmul(s, cfg, part, full, one, basis, 4, 2.0);
+    std::vector<double> scalars(4);
+    bad += !rpp::ops::tensor_pairing(s, cfg, rpp::make_scalar_batch(scalars.data()), part, one, basis, 4);
 
     rpp::basis::HallBasis<Arch> hall(W, D);
     auto lie = hall.to_lie_basis();

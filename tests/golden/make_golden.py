@@ -15,6 +15,8 @@ generator at test time.  Files written:
 * ``lie_<W>_<D>.npz``  -- Hall basis tables and the t2l / l2t CSC matrices
 * ``signature_w4d4.npz`` -- signatures of 8 paths of 32 steps (caller loop of ft_fmexp)
 * ``kat.json``         -- reverse_index and find_bracket known answers
+* ``shuffle_w3d4.npz`` -- the shuffle-algebra ops and tensor_pairing over the
+  degree-range cases of the reference's shuffle tests, plus small bases
 """
 from __future__ import annotations
 
@@ -133,6 +135,107 @@ def make_ops(ref: O.RefBridge, path: str) -> None:
     np.savez_compressed(path, width=W, depth=D, **out)
 
 
+# tests/rpp/cpu/single_thread/ops/st_mul_tests.cpp:222-268 (depth four):
+# (out, lhs, rhs)
+ST_MUL_CASES = [
+    ((0, 4), (0, 4), (0, 4)), ((0, 4), (1, 4), (0, 4)), ((0, 4), (0, 4), (1, 4)),
+    ((0, 4), (0, 2), (0, 4)), ((0, 4), (0, 4), (0, 2)), ((0, 4), (1, 3), (1, 2)),
+    ((2, 4), (0, 4), (0, 4)), ((0, 2), (0, 4), (0, 4)), ((1, 3), (0, 2), (1, 4)),
+]
+# st_fma_tests.cpp:285-311 and st_inplace_fma_tests.cpp:237-262: (out, a, b, c)
+ST_FMA_CASES = [
+    ((0, 4), (0, 4), (0, 4), (0, 4)), ((1, 3), (1, 3), (0, 2), (2, 4)),
+    ((1, 3), (1, 3), (1, 2), (1, 4)), ((0, 4), (2, 2), (0, 0), (0, 1)),
+]
+ST_INPLACE_CASES = [((0, 4), (0, 4), (0, 4)), ((1, 3), (1, 2), (1, 4)), ((1, 4), (0, 2), (1, 4)),
+                    ((0, 0), (0, 1), (0, 2))]
+# tests/rpp/shuffle_adjoint_test_helper.hpp:20-36 (out, op, arg) and the two
+# extra half-shuffle cases of half_shuffle_adjoint_test_helper.hpp:84-106.
+SH_ADJ_CASES = [
+    ((0, 4), (0, 4), (0, 4)), ((0, 4), (0, 0), (1, 2)), ((0, 4), (1, 2), (2, 3)),
+    ((0, 4), (1, 1), (3, 3)), ((0, 4), (3, 4), (0, 2)), ((0, 1), (0, 1), (3, 4)),
+    ((3, 4), (1, 2), (1, 2)), ((0, 4), (0, 0), (0, 0)), ((0, 4), (1, 2), (0, 0)),
+    ((0, 0), (2, 2), (2, 2)), ((0, 0), (1, 1), (2, 2)), ((1, 3), (0, 1), (2, 3)),
+    ((4, 4), (0, 0), (4, 4)),
+]
+HS_ADJ_EXTRA = [((1, 2), (1, 2), (2, 4)), ((0, 4), (0, 4), (0, 0))]
+# left_hs_mul_tests.cpp:136: every (lhs, rhs) pair of these ranges with the
+# full output, and every output range with full operands.
+HS_RANGES = [(0, 0), (0, 1), (1, 2), (2, 4), (0, 4)]
+PAIRING_CASES = [((0, 4), (0, 4)), ((1, 3), (0, 4)), ((0, 1), (2, 4)), ((2, 2), (2, 3)), ((4, 4), (0, 4))]
+
+
+def make_shuffle(ref: O.RefBridge, path: str) -> None:
+    """Inputs are stored once per basis; every case stores its ranges and the
+    reference's output, computed from `init` (NaN-free dyadic values)."""
+    rng = np.random.default_rng(31337)
+    out = {}
+    n = 2
+
+    def put(name, **arrays):
+        for k, v in arrays.items():
+            out[f"{name}/{k}"] = np.asarray(v)
+
+    W, D = 3, 4
+    dim = O.tensor_dim(W, D)
+    x, y, z, init = (tensor_batch(rng, n, dim) for _ in range(4))
+    out.update({"inputs/x": x, "inputs/y": y, "inputs/z": z, "inputs/init": init})
+    for i, rr in enumerate(ST_MUL_CASES):
+        res = init.copy()
+        ref.st_mul(W, D, res, x, y, rr, 0.75)
+        put(f"st_mul/{i}", ranges=np.array(rr), out=res, beta=0.75)
+    for i, rr in enumerate(ST_FMA_CASES):
+        res = init.copy()
+        ref.st_fma(W, D, res, z, x, y, rr, 0.5, -1.25)
+        put(f"st_fma/{i}", ranges=np.array(rr), out=res, alpha=0.5, beta=-1.25)
+    for i, rr in enumerate(ST_INPLACE_CASES):
+        res = z.copy()
+        ref.st_inplace_fma(W, D, res, x, y, rr, 0.5, 1.5)
+        put(f"st_inplace_fma/{i}", ranges=np.array(rr), out=res, alpha=0.5, beta=1.5)
+    hs = [((0, 4), l, r) for l in HS_RANGES for r in HS_RANGES] + [(o, (0, 4), (0, 4)) for o in HS_RANGES]
+    for i, rr in enumerate(hs):
+        res = init.copy()
+        ref.left_hs_mul(W, D, res, x, y, rr, 3.0)
+        put(f"left_hs_mul/{i}", ranges=np.array(rr), out=res, beta=3.0)
+    for i, rr in enumerate(SH_ADJ_CASES):
+        res = init.copy()
+        ref.st_adj_mul(W, D, res, x, y, rr)
+        put(f"st_adj_mul/{i}", ranges=np.array(rr), out=res)
+    for lmul in (1, 0):
+        name = "left_hs_adj_lmul" if lmul else "left_hs_adj_rmul"
+        for i, rr in enumerate(SH_ADJ_CASES + HS_ADJ_EXTRA):
+            # rr = (out, fixed operand, cotangent); the operator takes
+            # (integrator, integrand) = (fixed, cotangent) for lmul and
+            # (cotangent, fixed) for rmul.
+            res = init.copy()
+            if lmul:
+                ref.left_hs_adjoint(W, D, 1, res, x, y, (rr[0], rr[1], rr[2]))
+            else:
+                ref.left_hs_adjoint(W, D, 0, res, y, x, (rr[0], rr[2], rr[1]))
+            put(f"{name}/{i}", ranges=np.array(rr), out=res)
+    for i, fr in enumerate(PAIRING_CASES):
+        put(f"tensor_pairing/{i}", ranges=np.array(fr), out=ref.tensor_pairing(W, D, x, y, fr))
+    # the small bases of half_shuffle_adjoint_tests (width, depth): full views
+    for W2, D2 in [(1, 4), (2, 2), (4, 0)]:
+        dim2 = O.tensor_dim(W2, D2)
+        a, b, c = (tensor_batch(rng, n, dim2) for _ in range(3))
+        full = (0, D2)
+        key = f"small_{W2}_{D2}"
+        out[f"{key}/a"], out[f"{key}/b"], out[f"{key}/init"] = a, b, c
+        for name in ("st_mul", "left_hs_mul", "st_adj_mul", "left_hs_adj_lmul", "left_hs_adj_rmul"):
+            res = c.copy()
+            if name == "st_mul":
+                ref.st_mul(W2, D2, res, a, b, (full, full, full))
+            elif name == "left_hs_mul":
+                ref.left_hs_mul(W2, D2, res, a, b, (full, full, full))
+            elif name == "st_adj_mul":
+                ref.st_adj_mul(W2, D2, res, a, b, (full, full, full))
+            else:
+                ref.left_hs_adjoint(W2, D2, name.endswith("lmul"), res, a, b, (full, full, full))
+            out[f"{key}/{name}"] = res
+    np.savez_compressed(path, width=3, depth=4, **out)
+
+
 def make_lie(ref: O.RefBridge, W: int, D: int, path: str, with_spmv: bool) -> None:
     db, pairs = ref.hall_basis(W, D)
     t2l = ref.conversion_matrix(W, D, "t2l")
@@ -180,6 +283,7 @@ def main() -> None:
         make_lie(ref, W, D, os.path.join(HERE, f"lie_{W}_{D}.npz"), with_spmv=(W, D) in [(3, 4), (5, 5)])
     make_signature(ref, os.path.join(HERE, "signature_w4d4.npz"))
     make_kat(ref, os.path.join(HERE, "kat.json"))
+    make_shuffle(ref, os.path.join(HERE, "shuffle_w3d4.npz"))
 
 
 if __name__ == "__main__":

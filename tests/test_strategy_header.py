@@ -59,3 +59,15 @@ def test_tensor_to_lie_uses_begin_relative_views_and_caches_matrix(calls):
 def test_signature_entry(calls):
     assert "signature dtype=1 n=4 len=16 offsets=0 sig_stride=121 seed=0 grad=0" in calls
     assert calls[-1] == "failures=0"
+
+
+def test_shuffle_algebra(calls):
+    assert "st_mul dtype=1 n=4 out{s=128,0..4} x{s=128,1..2} y{s=121,1..1} a=0 b=0.5" in calls
+    assert "st_fma dtype=1 n=4 out{s=128,0..4} a{s=128,1..2} b{s=128,0..4} c{s=121,1..1} a=0.25 b=2" in calls
+    assert "st_inplace_fma dtype=1 n=4 a{s=128,0..4} b{s=121,1..1} c{s=128,1..2} a=1 b=0.5" in calls
+    assert "st_adj_mul dtype=1 n=4 out{s=128,1..2} x{s=128,0..4} y{s=121,1..1} a=0 b=0" in calls
+    assert "left_hs_mul dtype=1 n=4 out{s=128,0..4} x{s=128,1..2} y{s=121,1..1} a=0 b=3" in calls
+    assert "left_hs_adj_lmul dtype=1 n=4 out{s=128,1..2} x{s=128,0..4} y{s=121,1..1} a=0 b=1" in calls
+    assert "left_hs_adj_rmul dtype=1 n=4 out{s=128,1..2} x{s=128,0..4} y{s=121,1..1} a=0 b=2" in calls
+    assert "tensor_pairing dtype=1 n=4 result=set f{s=128,1..2} arg{s=121,1..1} a=0 b=0" in calls
+
