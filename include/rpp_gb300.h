@@ -23,7 +23,9 @@
  *    per-operation entry points allocate nothing after their plan / matrix
  *    handle is created; rpp_gb_signature allocates stream-ordered scratch
  *    (cudaMallocAsync / cudaFreeAsync on `stream`) for ragged batches and for
- *    states larger than shared memory.
+ *    states larger than shared memory, and the fused Lie <-> tensor steps
+ *    (rpp_gb_log_to_lie, rpp_gb_lie_to_tensor_exp) do the same for states
+ *    larger than shared memory.
  *  - dtype selects the scalar and accumulation type: RPP_GB_F32 (float data,
  *    float accumulation) or RPP_GB_F64 (double, double).
  */
@@ -273,6 +275,36 @@ int rpp_gb_matrix_destroy(rpp_gb_matrix* matrix);
 int rpp_gb_sparse_matrix_vector(const rpp_gb_matrix* matrix, rpp_gb_stream stream,
                                 int32_t dtype, const rpp_gb_vector_arg* out,
                                 const rpp_gb_vector_arg* arg, int64_t batch, double alpha);
+
+/* Fused steps either side of the signature.  Neither has a reference
+ * counterpart as one call: each computes the composition named below without
+ * writing the intermediate tensor to global memory.  The matrix handle must
+ * live on the plan's device; the tensor view [min_degree, max_degree] is
+ * clipped to the plan's depth. */
+
+/* rpp::ops::ft_log (include/rpp/operations/intermediate/ft_log.hpp:87-114)
+ * of `arg` into a tensor view over degrees [min_degree, max_degree], then
+ * rpp::ops::tensor_to_lie (include/rpp/operations/basic/tensor_to_lie.hpp:
+ * 65-103) with that view as the argument, i.e. rpp_gb_sparse_matrix_vector
+ * with arg = {log, begin = degree_begin[min_degree], size = degree_begin[
+ * max_degree+1] - begin}: out.begin()[r] = alpha * sum_c M[r][c] log[begin+c].
+ * With the tensor_to_lie matrix and a full view this is the log-signature. */
+int rpp_gb_log_to_lie(const rpp_gb_plan* plan, const rpp_gb_matrix* matrix, rpp_gb_stream stream,
+                      int32_t dtype, const rpp_gb_vector_arg* out, const rpp_gb_tensor_arg* arg,
+                      int32_t min_degree, int32_t max_degree, int64_t batch, double alpha);
+
+/* rpp::ops::lie_to_tensor (include/rpp/operations/basic/lie_to_tensor.hpp:
+ * 70-108) of `arg` into degrees [min_degree, max_degree] of a zero tensor X
+ * (X.begin()[r] = alpha * sum_c M[r][c] arg.begin()[c]), then
+ * rpp::ops::ft_exp (include/rpp/operations/intermediate/ft_exp.hpp) of X into
+ * `out` when `multiplier` is NULL, else rpp::ops::ft_fmexp (ft_fmexp.hpp:
+ * 91-121): out = multiplier (x) exp(X); out must not alias multiplier.  With
+ * the lie_to_tensor matrix this is one step of a path given by Lie
+ * increments. */
+int rpp_gb_lie_to_tensor_exp(const rpp_gb_plan* plan, const rpp_gb_matrix* matrix, rpp_gb_stream stream,
+                             int32_t dtype, const rpp_gb_tensor_arg* out,
+                             const rpp_gb_tensor_arg* multiplier, const rpp_gb_vector_arg* arg,
+                             int32_t min_degree, int32_t max_degree, int64_t batch, double alpha);
 
 /* Hall basis and conversion matrices built natively (restating
  * include/rpp/basis/hall_basis.hpp:35-88, include/rpp/basis/

@@ -33,7 +33,7 @@ __all__ = [
     "tensor_set_identity", "tensor_add_identity", "sparse_matrix_vector_product",
     "tensor_to_lie", "lie_to_tensor", "signature", "signature_backward", "signature_tune", "exp_letter_vjp",
     "st_mul", "st_fma", "st_inplace_fma", "st_adj_mul", "left_hs_mul", "left_hs_adj_lmul", "left_hs_adj_rmul",
-    "tensor_pairing", "make_scalar_batch", "build", "library",
+    "tensor_pairing", "make_scalar_batch", "tensor_log_to_lie", "lie_to_tensor_exp", "build", "library",
 ]
 
 
@@ -603,6 +603,35 @@ def tensor_to_lie(strategy, config, out, arg, lie_basis, tensor_basis, num_batch
 def lie_to_tensor(strategy, config, out, arg, tensor_basis, lie_basis, num_batches, matrix) -> Error:
     """include/rpp/operations/basic/lie_to_tensor.hpp:76-108"""
     return sparse_matrix_vector_product(strategy, config, out, arg, tensor_basis, lie_basis, num_batches, matrix)
+
+
+def tensor_log_to_lie(strategy, config, out, arg, lie_basis, tensor_basis, num_batches, matrix,
+                      log_degrees=None, alpha=1.0) -> Error:
+    """Fused ft_log + tensor_to_lie (rpp_gb_log_to_lie): out (a Lie batch) =
+    alpha * M * log(arg) on the tensor view ``log_degrees`` (default: every
+    degree), without writing the log tensor."""
+    _check_batches(strategy, out, arg)
+    lo, hi = log_degrees if log_degrees is not None else (0, tensor_basis.depth)
+    lib = _lib.load()
+    o = _vec(out, lie_basis)
+    return _status(lib.rpp_gb_log_to_lie(tensor_basis.plan(strategy.device), matrix.handle(strategy.device),
+                                         _cfg(config).handle(strategy.device), strategy.dtype_code(),
+                                         ctypes.byref(o), _p(arg), int(lo), int(hi), num_batches, alpha))
+
+
+def lie_to_tensor_exp(strategy, config, out, multiplier, arg, tensor_basis, lie_basis, num_batches, matrix,
+                      tensor_degrees=None, alpha=1.0) -> Error:
+    """Fused lie_to_tensor + ft_exp / ft_fmexp (rpp_gb_lie_to_tensor_exp):
+    X = alpha * M * arg on the tensor view ``tensor_degrees`` (default: every
+    degree) of a zero tensor, out = exp(X) or multiplier (x) exp(X)."""
+    _check_batches(strategy, out, multiplier, arg)
+    lo, hi = tensor_degrees if tensor_degrees is not None else (0, tensor_basis.depth)
+    lib = _lib.load()
+    a = _vec(arg, lie_basis)
+    return _status(lib.rpp_gb_lie_to_tensor_exp(tensor_basis.plan(strategy.device), matrix.handle(strategy.device),
+                                                _cfg(config).handle(strategy.device), strategy.dtype_code(), _p(out),
+                                                _p(multiplier), ctypes.byref(a), int(lo), int(hi), num_batches,
+                                                alpha))
 
 
 # --------------------------------------------------------------------------

@@ -77,6 +77,8 @@ SIGNATURES = {
     "rpp_gb_matrix_create": [ctypes.POINTER(_vp), _i32, _i64, _i64, _i64, _I64P, _I64P, _DBLP, _i32],
     "rpp_gb_matrix_destroy": [_vp],
     "rpp_gb_sparse_matrix_vector": [_vp, _vp, _i32, _V, _V, _i64, _dbl],
+    "rpp_gb_log_to_lie": [_vp, _vp, _vp, _i32, _V, _P, _i32, _i32, _i64, _dbl],
+    "rpp_gb_lie_to_tensor_exp": [_vp, _vp, _vp, _i32, _P, _P, _V, _i32, _i32, _i64, _dbl],
     "rpp_gb_lie_basis": [_i32, _i32, _I64P, _I64P, _I64P],
     "rpp_gb_conversion_matrix": [_i32, _i32, _i32, _I64P, _I64P, _I64P, _I64P, _I64P, _DBLP],
     "rpp_gb_signature": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp],

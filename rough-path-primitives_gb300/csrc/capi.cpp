@@ -459,6 +459,116 @@ int run_pairing(const rpp_gb_plan* plan, cudaStream_t s, void* result, const rpp
 }
 
 
+// Fused Lie <-> tensor steps.  When the work tensors exceed shared memory the
+// unfused kernels are composed through a stream-ordered scratch batch.
+bool degree_view(const rpp_gb::Geometry& g, int32_t lo, int32_t hi, int& vlo, int& vhi) {
+    if (lo < 0 || hi < lo || lo > g.depth) return false;
+    vlo = lo;
+    vhi = std::min<int32_t>(hi, g.depth);
+    return true;
+}
+
+bool check_vector(const rpp_gb_vector_arg* v, int64_t batch, const char* name) {
+    if (!v) {
+        fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + " is NULL");
+        return false;
+    }
+    if (v->begin < 0 || v->size < 0) {
+        fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + ": negative view offset or size");
+        return false;
+    }
+    if (!v->data) {
+        fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + ": NULL data");
+        return false;
+    }
+    if (batch > 1 && v->stride < v->begin + v->size) {
+        fail(RPP_GB_INVALID_ARGUMENT, std::string(name) + ": stride shorter than the view");
+        return false;
+    }
+    return true;
+}
+
+template <typename T>
+int run_log_to_lie(const rpp_gb_plan* plan, const rpp_gb_matrix* matrix, cudaStream_t s,
+                   const rpp_gb_vector_arg* out, const rpp_gb_tensor_arg* arg, int lo, int hi, int64_t batch,
+                   double alpha) {
+    const auto& g = plan->geometry;
+    const auto& m = matrix->csr;
+    rpp_gb::TArg<T> x;
+    if (!to_targ(arg, g, true, batch, x, "arg") || !check_vector(out, batch, "out"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    const int64_t view = static_cast<int64_t>(g.db[hi + 1]) - g.db[lo];
+    if (m.rows > out->size) return fail(RPP_GB_OUT_OF_BOUNDS, "matrix has more rows than the output view");
+    if (m.cols_dim > view) return fail(RPP_GB_OUT_OF_BOUNDS, "matrix has more columns than the log view");
+    T* o = static_cast<T*>(out->data) + out->begin;
+    if (rpp_gb::log_to_lie_smem(g, sizeof(T)) <= static_cast<size_t>(plan->device.max_smem_optin))
+        return cuda_status(rpp_gb::launch_log_to_lie<T>(g, plan->device, s, m, x, lo, hi, o, out->stride, out->size,
+                                                        batch, alpha),
+                           "log-to-Lie kernel");
+    T* tmp = nullptr;
+    const size_t bytes = static_cast<size_t>(batch) * g.dim * sizeof(T);
+    cudaError_t err = cudaMallocAsync(reinterpret_cast<void**>(&tmp), bytes, s);
+    if (err != cudaSuccess) return cuda_status(err, "log-to-Lie scratch");
+    rpp_gb::TArg<T> t{tmp, static_cast<int64_t>(g.dim), lo, hi};
+    err = rpp_gb::launch_intermediate<T>(g, plan->device, s, rpp_gb::IntermediateKind::Log, t, x, rpp_gb::TArg<T>{},
+                                         batch);
+    if (err == cudaSuccess)
+        err = rpp_gb::launch_spmm<T>(m, plan->device, s, o, out->stride, out->size, tmp + g.db[lo], g.dim, view, batch,
+                                     alpha);
+    const cudaError_t ferr = cudaFreeAsync(tmp, s);
+    return cuda_status(err != cudaSuccess ? err : ferr, "log-to-Lie (composed)");
+}
+
+template <typename T>
+int run_lie_exp(const rpp_gb_plan* plan, const rpp_gb_matrix* matrix, cudaStream_t s, const rpp_gb_tensor_arg* out,
+                const rpp_gb_tensor_arg* mult, const rpp_gb_vector_arg* arg, int lo, int hi, int64_t batch,
+                double alpha) {
+    const auto& g = plan->geometry;
+    const auto& m = matrix->csr;
+    rpp_gb::TArg<T> o, mm;
+    if (!to_targ(out, g, true, batch, o, "out", true) || !to_targ(mult, g, false, batch, mm, "multiplier") ||
+        !check_vector(arg, batch, "arg"))
+        return static_cast<int>(RPP_GB_INVALID_ARGUMENT);
+    if (mult && out->data == mult->data) return fail(RPP_GB_INVALID_ARGUMENT, "out must not alias multiplier");
+    const int64_t view = static_cast<int64_t>(g.db[hi + 1]) - g.db[lo];
+    if (m.rows > view) return fail(RPP_GB_OUT_OF_BOUNDS, "matrix has more rows than the tensor view");
+    if (m.cols_dim > arg->size) return fail(RPP_GB_OUT_OF_BOUNDS, "matrix has more columns than the argument view");
+    const T* lie = static_cast<const T*>(arg->data) + arg->begin;
+    if (rpp_gb::lie_exp_smem(g, sizeof(T), mult != nullptr) <= static_cast<size_t>(plan->device.max_smem_optin) &&
+        m.cols_dim <= static_cast<int64_t>(g.dim))
+        return cuda_status(
+            rpp_gb::launch_lie_exp<T>(g, plan->device, s, m, lie, arg->stride, lo, hi, o, mm, batch, alpha),
+            "Lie-exp kernel");
+    T* tmp = nullptr;
+    const size_t bytes = static_cast<size_t>(batch) * g.dim * sizeof(T);
+    cudaError_t err = cudaMallocAsync(reinterpret_cast<void**>(&tmp), bytes, s);
+    if (err != cudaSuccess) return cuda_status(err, "Lie-exp scratch");
+    err = cudaMemsetAsync(tmp, 0, bytes, s);
+    if (err == cudaSuccess)
+        err = rpp_gb::launch_spmm<T>(m, plan->device, s, tmp + g.db[lo], g.dim, view, lie, arg->stride, arg->size,
+                                     batch, alpha);
+    if (err == cudaSuccess) {
+        rpp_gb::TArg<T> t{tmp, static_cast<int64_t>(g.dim), std::max(1, lo), hi};
+        err = rpp_gb::launch_intermediate<T>(g, plan->device, s,
+                                             mult ? rpp_gb::IntermediateKind::FMExp : rpp_gb::IntermediateKind::Exp,
+                                             o, t, mm, batch);
+    }
+    const cudaError_t ferr = cudaFreeAsync(tmp, s);
+    return cuda_status(err != cudaSuccess ? err : ferr, "Lie-exp (composed)");
+}
+
+template <typename F>
+int with_plan_matrix(const rpp_gb_plan* plan, const rpp_gb_matrix* matrix, int32_t dtype, int64_t batch,
+                     int32_t min_degree, int32_t max_degree, int& lo, int& hi, F&& body) {
+    if (!matrix) return fail(RPP_GB_INVALID_ARGUMENT, "matrix is NULL");
+    if (plan && matrix->device != plan->device.device)
+        return fail(RPP_GB_INVALID_ARGUMENT, "matrix and plan live on different devices");
+    if (plan && !degree_view(plan->geometry, min_degree, max_degree, lo, hi))
+        return fail(RPP_GB_INVALID_ARGUMENT, "degree range must satisfy 0 <= min <= max, min <= depth");
+    return with_plan(plan, dtype, batch, std::forward<F>(body));
+}
+
+
 extern "C" {
 
 const char* rpp_gb_last_error_string(void) { return g_last_error.c_str(); }
@@ -791,6 +901,30 @@ int rpp_gb_sparse_matrix_vector(const rpp_gb_matrix* matrix, rpp_gb_stream strea
                                          out->size, static_cast<const float*>(arg->data) + arg->begin, arg->stride,
                                          arg->size, batch, alpha);
     return cuda_status(err, "spmm kernel");
+}
+
+int rpp_gb_log_to_lie(const rpp_gb_plan* plan, const rpp_gb_matrix* matrix, rpp_gb_stream stream, int32_t dtype,
+                      const rpp_gb_vector_arg* out, const rpp_gb_tensor_arg* arg, int32_t min_degree,
+                      int32_t max_degree, int64_t batch, double alpha) {
+    int lo = 0, hi = -1;
+    return with_plan_matrix(plan, matrix, dtype, batch, min_degree, max_degree, lo, hi, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_log_to_lie<double>(plan, matrix, s, out, arg, lo, hi, batch, alpha)
+                                   : run_log_to_lie<float>(plan, matrix, s, out, arg, lo, hi, batch, alpha);
+    });
+}
+
+int rpp_gb_lie_to_tensor_exp(const rpp_gb_plan* plan, const rpp_gb_matrix* matrix, rpp_gb_stream stream,
+                             int32_t dtype, const rpp_gb_tensor_arg* out, const rpp_gb_tensor_arg* multiplier,
+                             const rpp_gb_vector_arg* arg, int32_t min_degree, int32_t max_degree, int64_t batch,
+                             double alpha) {
+    int lo = 0, hi = -1;
+    return with_plan_matrix(plan, matrix, dtype, batch, min_degree, max_degree, lo, hi, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64
+                   ? run_lie_exp<double>(plan, matrix, s, out, multiplier, arg, lo, hi, batch, alpha)
+                   : run_lie_exp<float>(plan, matrix, s, out, multiplier, arg, lo, hi, batch, alpha);
+    });
 }
 
 int rpp_gb_lie_basis(int32_t width, int32_t depth, int64_t* true_size, int64_t* degree_begin, int64_t* pairs) {

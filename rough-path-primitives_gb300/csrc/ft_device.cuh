@@ -1,0 +1,120 @@
+// ft_device.cuh -- device building blocks shared by the per-operation kernels
+// (ft_ops.cu) and the fused Lie <-> tensor kernels (lie_fused.cu): level-wise
+// products over degree-range operands and the Horner intermediates
+// (exp / fmexp / log) on a work buffer in shared or global memory.
+#pragma once
+
+#include "common.cuh"
+#include "ops.hpp"
+
+namespace rpp_gb {
+namespace ftdev {
+
+template <typename T>
+struct Opnd {
+    const T* p;
+    int lo;
+    int hi;
+};
+
+template <typename T>
+__device__ __forceinline__ T split_sum(const Geometry& G, const Opnd<T>& L, const Opnd<T>& R, int n,
+                                       uint32_t i) {
+    const int kmin = imax(imax(R.lo, 0), n - L.hi);
+    const int kmax = imin(imin(R.hi, n), n - L.lo);
+    T acc = T(0);
+    if (kmin > kmax) return acc;
+    uint32_t q = i, r = 0, p = 1;
+    for (int k = 0; k < kmin; ++k) {
+        uint32_t qq, rr;
+        G.divw.divmod(q, qq, rr);
+        r += rr * p;
+        p *= static_cast<uint32_t>(G.width);
+        q = qq;
+    }
+    for (int k = kmin;; ++k) {
+        acc = fma(L.p[G.db[n - k] + q], R.p[G.db[k] + r], acc);
+        if (k == kmax) break;
+        uint32_t qq, rr;
+        G.divw.divmod(q, qq, rr);
+        r += rr * p;
+        p *= static_cast<uint32_t>(G.width);
+        q = qq;
+    }
+    return acc;
+}
+
+// Copy levels [lo, hi] of a tensor into the same positions of a shared buffer.
+template <typename T>
+__device__ __forceinline__ void stage(T* dst, const T* src, int lo, int hi, const Geometry& G) {
+    if (lo > hi) return;
+    const uint32_t b = G.db[lo], e = G.db[hi + 1];
+    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) dst[i] = src[i];
+}
+
+// out[n] = alpha*add[n] + beta * L (x) R at level n, for n in [lo, hi], top
+// degree first; `sync` puts a barrier after each degree (needed when L or R
+// alias the destination in global memory).
+template <typename T>
+__device__ void product_levels(const Geometry& G, T* dst, int lo, int hi, const Opnd<T>& add,
+                               T alpha, const Opnd<T>& L, const Opnd<T>& R, T beta, bool sync) {
+    for (int n = hi; n >= lo; --n) {
+        const uint32_t size = G.pw[n];
+        const uint32_t base = G.db[n];
+        const bool has_add = add.p != nullptr && add.lo <= n && n <= add.hi;
+        for (uint32_t i = threadIdx.x; i < size; i += blockDim.x) {
+            T val = beta * split_sum(G, L, R, n, i);
+            if (has_add) val = fma(alpha, add.p[base + i], val);
+            dst[base + i] = val;
+        }
+        if (sync) __syncthreads();
+    }
+}
+
+// One Horner intermediate on work buffer `o` (shared or global), following
+// include/rpp/gpu/block/operations/intermediate/ft_exp.hpp:66-81,
+// ft_fmexp.hpp:61-83 and ft_log.hpp:66-83.  Every in-place product reads only
+// lower degrees of `o` (the exponent/argument is truncated to degree >= 1), so
+// a barrier per degree, top degree first, keeps it exact.
+template <typename T>
+__device__ void intermediate_one(const Geometry& G, IntermediateKind kind, T* o, int olo, int ohi,
+                                 Opnd<T> X, Opnd<T> M) {
+    const int D = G.depth;
+    // initialisation: set_identity / assign / set_constant
+    if (olo <= ohi) {
+        const uint32_t bgn = G.db[olo], end = G.db[ohi + 1];
+        for (uint32_t i = bgn + threadIdx.x; i < end; i += blockDim.x) {
+            T v = T(0);
+            if (kind == IntermediateKind::FMExp) {
+                const uint32_t mb = M.lo <= M.hi ? G.db[M.lo] : 0, me = M.lo <= M.hi ? G.db[M.hi + 1] : 0;
+                if (i >= mb && i < me) v = M.p[i];
+            }
+            o[i] = v;
+        }
+    }
+    __syncthreads();
+    if (kind == IntermediateKind::Exp && threadIdx.x == 0 && olo == 0) o[0] = T(1);
+    __syncthreads();
+    const Opnd<T> none{nullptr, 1, 0};
+    for (int d = D; d > 0; --d) {
+        const int tmax = D - d + 1;
+        const Opnd<T> Xt{X.p, imax(1, X.lo), imin(X.hi, tmax)};
+        const T inv = T(1) / static_cast<T>(d);
+        if (kind == IntermediateKind::Exp) {
+            product_levels(G, o, olo, ohi, none, T(0), Opnd<T>{o, olo, ohi}, Xt, inv, true);
+            if (threadIdx.x == 0 && olo == 0) o[0] += T(1);
+            __syncthreads();
+        } else if (kind == IntermediateKind::FMExp) {
+            product_levels(G, o, olo, ohi, M, T(1), Opnd<T>{o, olo, ohi}, Xt, inv, true);
+        } else {
+            const T val = ((d % 2 == 0) ? T(-1) : T(1)) / static_cast<T>(d);
+            if (threadIdx.x == 0 && olo == 0) o[0] += val;
+            __syncthreads();
+            const int thi = imin(ohi, tmax);
+            product_levels(G, o, olo, thi, none, T(0), Opnd<T>{o, olo, thi}, Xt, T(1), true);
+        }
+    }
+}
+
+}  // namespace ftdev
+}  // namespace rpp_gb

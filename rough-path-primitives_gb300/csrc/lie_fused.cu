@@ -1,0 +1,163 @@
+// lie_fused.cu -- the steps either side of the signature, fused per tensor.
+//
+// Log-signature epilogue: out = alpha * T2L * log(x), where log is
+// rpp::ops::ft_log (include/rpp/operations/intermediate/ft_log.hpp:87-114)
+// on the degree range [lo, hi] and T2L is the tensor_to_lie matrix
+// (include/rpp/operations/basic/tensor_to_lie.hpp:65-103, built by
+// include/rpp/sparse/t2l_matrix.hpp:57-142) applied to that view with the
+// begin-relative indexing of the CPU strategy's SpMV.  The reference composes
+// two launches with the full log tensor in between; here the log stays in
+// shared memory and only the Lie coefficients are written.
+//
+// Lie-increment step: X = alpha * L2T * lambda written to degrees [lo, hi] of a
+// zero tensor (rpp::ops::lie_to_tensor, lie_to_tensor.hpp:70-108, matrix from
+// include/rpp/sparse/l2t_matrix.hpp:58-114), then out = exp(X)
+// (ft_exp.hpp) or out = M (x) exp(X) (ft_fmexp.hpp:91-121): one log-ODE step of
+// a path given by Lie increments.  X never leaves shared memory.
+//
+// Both kernels hold one tensor of the batch per CTA (grid-stride) and need
+// the work tensors in shared memory; the host composes the unfused kernels
+// for states that do not fit.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ft_device.cuh"
+#include "launch_util.cuh"
+#include "ops.hpp"
+
+namespace rpp_gb {
+namespace {
+
+using namespace ftdev;
+
+template <typename T>
+__device__ __forceinline__ const T* csr_vals(const CsrDevice& m);
+template <>
+__device__ __forceinline__ const double* csr_vals<double>(const CsrDevice& m) {
+    return m.values64;
+}
+template <>
+__device__ __forceinline__ const float* csr_vals<float>(const CsrDevice& m) {
+    return m.values32;
+}
+
+// y[r] = alpha * sum_e val[e] x[col[e]] for r < rows; zeros up to `zero_to`
+// when the matrix came from CSC (its product zeroes the whole output view).
+template <typename T>
+__device__ __forceinline__ void csr_rows(const CsrDevice& m, const T* __restrict__ x, T* y, int64_t zero_to, T alpha) {
+    const T* vals = csr_vals<T>(m);
+    const int64_t end = m.zero_rest ? zero_to : m.rows;
+    for (int64_t r = threadIdx.x; r < end; r += blockDim.x) {
+        T acc = T(0);
+        if (r < m.rows) {
+            const int32_t e0 = __ldg(m.offsets + r), e1 = __ldg(m.offsets + r + 1);
+            for (int32_t e = e0; e < e1; ++e) acc = fma(__ldg(vals + e), x[__ldg(m.cols + e)], acc);
+        }
+        y[r] = alpha * acc;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_log_to_lie(Geometry G, CsrDevice m, TArg<T> x, int lo, int hi, T* out,
+                                                   int64_t out_stride, int64_t out_size, int64_t batch, T alpha) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* s_x = reinterpret_cast<T*>(smem_raw);
+    T* s_log = s_x + G.dim;
+    const Opnd<T> none{nullptr, 1, 0};
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        Opnd<T> X{x.at(b), imax(1, x.lo), imin(x.hi, G.depth)};
+        stage(s_x, X.p, X.lo, X.hi, G);
+        __syncthreads();
+        X.p = s_x;
+        intermediate_one(G, IntermediateKind::Log, s_log, lo, hi, X, none);
+        __syncthreads();
+        csr_rows(m, s_log + G.db[lo], out + b * out_stride, out_size, alpha);
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const T* lie, int64_t lie_stride, int lo,
+                                                int hi, TArg<T> out, TArg<T> mult, int64_t batch, T alpha) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* s_x = reinterpret_cast<T*>(smem_raw);
+    T* s_o = s_x + G.dim;  // also holds the Lie vector until X is formed
+    T* s_m = s_o + G.dim;
+    const int ohi = imin(out.hi, G.depth);
+    const bool fm = mult.p != nullptr;
+    const uint32_t view = G.db[hi + 1] - G.db[lo];
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        const T* l = lie + b * lie_stride;
+        for (int64_t i = threadIdx.x; i < m.cols_dim; i += blockDim.x) s_o[i] = l[i];
+        for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) s_x[i] = T(0);
+        Opnd<T> M{nullptr, 1, 0};
+        if (fm) {
+            M = {mult.at(b), mult.lo, imin(mult.hi, G.depth)};
+            stage(s_m, M.p, M.lo, M.hi, G);
+            M.p = s_m;
+        }
+        __syncthreads();
+        csr_rows(m, s_o, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
+        __syncthreads();
+        const Opnd<T> X{s_x, imax(1, lo), hi};
+        intermediate_one(G, fm ? IntermediateKind::FMExp : IntermediateKind::Exp, s_o, out.lo, ohi, X, M);
+        __syncthreads();
+        T* o = out.at(b);
+        if (out.lo <= ohi)
+            for (uint32_t i = G.db[out.lo] + threadIdx.x; i < G.db[ohi + 1]; i += blockDim.x) o[i] = s_o[i];
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+size_t log_to_lie_smem(const Geometry& g, size_t elem) { return 2 * static_cast<size_t>(g.dim) * elem; }
+size_t lie_exp_smem(const Geometry& g, size_t elem, bool fm) {
+    return (fm ? 3 : 2) * static_cast<size_t>(g.dim) * elem;
+}
+
+template <typename T>
+cudaError_t launch_log_to_lie(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const CsrDevice& m,
+                              TArg<T> x, int lo, int hi, T* out, int64_t out_stride, int64_t out_size, int64_t batch,
+                              double alpha) {
+    if (batch <= 0) return cudaSuccess;
+    constexpr auto kernel = k_log_to_lie<T>;
+    cudaError_t err = allow_large_smem<kernel>(dev);
+    if (err != cudaSuccess) return err;
+    const size_t smem = log_to_lie_smem(g, sizeof(T));
+    if (smem > static_cast<size_t>(dev.max_smem_optin)) return cudaErrorInvalidConfiguration;
+    const int threads = threads_for(g.pw[g.depth]);
+    dim3 grid;
+    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+    kernel<<<grid, threads, smem, s>>>(g, m, x, lo, hi, out, out_stride, out_size, batch, static_cast<T>(alpha));
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_lie_exp(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const CsrDevice& m,
+                           const T* lie, int64_t lie_stride, int lo, int hi, TArg<T> out, TArg<T> mult,
+                           int64_t batch, double alpha) {
+    if (batch <= 0) return cudaSuccess;
+    constexpr auto kernel = k_lie_exp<T>;
+    cudaError_t err = allow_large_smem<kernel>(dev);
+    if (err != cudaSuccess) return err;
+    const size_t smem = lie_exp_smem(g, sizeof(T), mult.p != nullptr);
+    if (smem > static_cast<size_t>(dev.max_smem_optin) || m.cols_dim > static_cast<int64_t>(g.dim))
+        return cudaErrorInvalidConfiguration;
+    const int threads = threads_for(g.pw[g.depth]);
+    dim3 grid;
+    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+    kernel<<<grid, threads, smem, s>>>(g, m, lie, lie_stride, lo, hi, out, mult, batch, static_cast<T>(alpha));
+    return cudaGetLastError();
+}
+
+#define RPP_GB_INSTANTIATE_LIE_FUSED(T)                                                                           \
+    template cudaError_t launch_log_to_lie<T>(const Geometry&, const DeviceInfo&, cudaStream_t, const CsrDevice&, \
+                                              TArg<T>, int, int, T*, int64_t, int64_t, int64_t, double);          \
+    template cudaError_t launch_lie_exp<T>(const Geometry&, const DeviceInfo&, cudaStream_t, const CsrDevice&,    \
+                                           const T*, int64_t, int, int, TArg<T>, TArg<T>, int64_t, double);
+
+RPP_GB_INSTANTIATE_LIE_FUSED(float)
+RPP_GB_INSTANTIATE_LIE_FUSED(double)
+
+}  // namespace rpp_gb

@@ -114,6 +114,24 @@ template <typename T>
 cudaError_t launch_pairing(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, T* result, TArg<T> f, TArg<T> a,
                            int64_t batch);
 
+// Fused Lie <-> tensor steps (lie_fused.cu).  Both need their work tensors in
+// shared memory: *_smem gives the bytes, the caller composes the unfused
+// kernels when it exceeds the device's limit.
+size_t log_to_lie_smem(const Geometry& g, size_t elem);
+size_t lie_exp_smem(const Geometry& g, size_t elem, bool fm);
+
+// out (begin-relative, out_size coefficients) = alpha * M * log(x)|[lo, hi]
+template <typename T>
+cudaError_t launch_log_to_lie(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const CsrDevice& m,
+                              TArg<T> x, int lo, int hi, T* out, int64_t out_stride, int64_t out_size, int64_t batch,
+                              double alpha);
+
+// out = exp(X) or mult (x) exp(X), X = alpha * M * lie on degrees [lo, hi]
+template <typename T>
+cudaError_t launch_lie_exp(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const CsrDevice& m,
+                           const T* lie, int64_t lie_stride, int lo, int hi, TArg<T> out, TArg<T> mult,
+                           int64_t batch, double alpha);
+
 // Fused signature kernels.
 struct PathBatch {
     const int64_t* offsets;  // device, batch + 1 (or nullptr)
