@@ -316,7 +316,7 @@ def workload_ragged(pkg, torch, args, peak):
     _line("uneven-length signatures paths/sec (W8 D4, 10k paths, L~U[16,2048]), FP64 + FP32 in one graph",
           B / (ms / 1e3), "paths/s", ms, "f64+f32",
           {"workload": "ragged_w8_d4_b10000", "total_increments": steps_total,
-           "graph": "fp64 launch + fp32 launch", "threads_per_cta": {"f64": t64[1], "f32": t32[1]}},
+           "graph": "fp64 launch + fp32 launch", "schedule": {"f64": t64[1], "f32": t32[1]}},
           extra={"fp64_ms": ms64, "fp32_ms": ms32, "fp64_paths_per_s": B / (ms64 / 1e3),
                  "fp32_paths_per_s": B / (ms32 / 1e3), "fp32_max_rel_err_vs_fp64": err32,
                  "fp64_roofline_frac": flops64 / (ms64 / 1e3) / 1e12 / peak if peak else None})
@@ -337,7 +337,8 @@ def workload_fwd_bwd(pkg, torch, args, peak, W, D, B, L, name):
         torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad),
         args.steps, args.warmup, torch.cuda.current_stream())
     _line(f"signature fwd+bwd paths/sec (W{W} D{D} L{L} FP64)", B / (ms / 1e3), "paths/s", ms, "f64",
-          {"workload": name, "batch": B, "length": L, "threads_per_cta": threads},
+          {"workload": name, "batch": B, "length": L, "threads_per_cta": threads & 1023,
+           "ctas_per_sm_cap": threads >> 10},
           flops=2.0 * 4 * L * step_fma(W, D) * B, peak=peak)
 
 
@@ -642,7 +643,8 @@ def main():
                    "batch_per_gpu": batch, "length": LENGTH, "increments": "N(0,1/256) iid",
                    "seed_functional": "U[-1,1]", "l2": "inputs+outputs 340 MB > L2 (no flush needed)",
                    "kernel": "fused forward+reverse, one launch per step", "parallelism": f"replicas x{world}",
-                   "schedule": {"threads_per_cta": tuned_threads, "chosen_by": "rpp_gb_signature_tune"}},
+                   "schedule": {"threads_per_cta": tuned_threads & 1023, "ctas_per_sm_cap": tuned_threads >> 10,
+                                "chosen_by": "rpp_gb_signature_tune"}},
         "roofline": {"bound": "fp64_fma", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": (achieved / fp64_peak) if fp64_peak else None, "traffic": None,
                      "peak_source": "measured in-run (rpp_gb_fma_peak, FP64 FMA chains)",

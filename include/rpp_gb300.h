@@ -373,12 +373,14 @@ int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream strea
 
 /* Autotuner for rpp_gb_signature (no reference counterpart): runs the same
  * call once per candidate schedule (threads per CTA of the shared-memory
- * kernel) on the caller's own inputs, times each with CUDA events on
- * `stream`, and records the fastest for this (device, width, depth, dtype,
- * outputs requested, ragged or not); later rpp_gb_signature calls with that
- * key use it.  Synchronises the stream (not capturable); leaves the chosen
- * schedule's outputs in sig/grad.  *threads and *ms (may be NULL) receive the
- * choice and its time per launch. */
+ * kernel, optionally with fewer CTAs per SM than fit, which trades occupancy
+ * for a fuller last wave) on the caller's own inputs, times each with CUDA
+ * events on `stream`, and records the fastest for this (device, width, depth,
+ * dtype, outputs requested, ragged or not); later rpp_gb_signature calls with
+ * that key use it.  Synchronises the stream (not capturable); leaves the
+ * chosen schedule's outputs in sig/grad.  *threads and *ms (may be NULL)
+ * receive the choice and its time per launch: threads per CTA in the low 10
+ * bits of *threads, the cap on CTAs per SM (0 = none) above them. */
 int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
                           const void* incr, const int64_t* offsets, int64_t length, int64_t batch,
                           void* sig, int64_t sig_stride, const void* seed, int64_t seed_stride,

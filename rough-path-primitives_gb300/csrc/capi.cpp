@@ -333,9 +333,11 @@ int run_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const 
                        "signature kernel");
 }
 
-// Autotuner: time each candidate CTA size on the caller's own inputs (one
-// warm-up and two timed launches each, CUDA events on `s`), keep the fastest.
-// Candidates that cannot launch for this shape are skipped.
+// Autotuner: time each candidate schedule (CTA size, optionally with a cap on
+// CTAs per SM: see launch_width) on the caller's own inputs (one warm-up and
+// two timed launches each, CUDA events on `s`), keep the fastest.  Candidates
+// that cannot launch for this shape, or whose cap would not lower the
+// residency, are skipped.
 template <typename T>
 int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const void* incr, const int64_t* offsets,
                    int64_t length, int64_t batch, void* sig, int64_t sig_stride, const void* seed,
@@ -343,13 +345,19 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
     if (int rc = check_signature_args<T>(plan, incr, offsets, length, sig, sig_stride, seed, seed_stride, grad,
                                          true))
         return rc;
-    static const int candidates[] = {128, 192, 256, 320, 384, 448, 512};
+    static const int sizes[] = {128, 192, 256, 320, 384, 512};
+    static const int caps[] = {0, 3, 2};
+    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 3];
+    int ncand = 0;
+    for (int c : caps)
+        for (int t : sizes) candidates[ncand++] = t | (c << 10);
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return fail(RPP_GB_OUT_OF_RESOURCES, "cudaEventCreate failed");
     int best = 0;
     float best_ms = 0.f;
-    for (int t : candidates) {
+    for (int ci = 0; ci < ncand; ++ci) {
+        const int t = candidates[ci];
         int rc = RPP_GB_SUCCESS;
         for (int rep = 0; rep < 3 && rc == RPP_GB_SUCCESS; ++rep) {
             if (rep == 1) cudaEventRecord(e0, s);
@@ -430,10 +438,8 @@ int run_shuffle_adjoint(const rpp_gb_plan* plan, cudaStream_t s, rpp_gb::Shuffle
     const bool swap = kind == rpp_gb::ShuffleAdjKind::HalfR;
     const auto& fixed = swap ? a : p;
     const auto& cot = swap ? p : a;
-    const auto ord = rpp_gb::shuffle_adjoint_order(g, kind, o.lo, o.hi, fixed.lo, fixed.hi, cot.lo, cot.hi);
-    return cuda_status(
-        rpp_gb::launch_shuffle_adjoint<T>(g, plan->device, s, kind, o, fixed, cot, batch, beta, ord),
-        "shuffle adjoint kernel");
+    return cuda_status(rpp_gb::launch_shuffle_adjoint<T>(g, plan->device, s, kind, o, fixed, cot, batch, beta),
+                       "shuffle adjoint kernel");
 }
 
 int run_shuffle_adjoint_any(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,

@@ -98,17 +98,17 @@ struct ShuffleOrder {
 
 ShuffleOrder shuffle_product_order(const Geometry& g, int out_lo, int out_hi);
 ShuffleOrder shuffle_adjoint_order(const Geometry& g, ShuffleAdjKind kind, int out_lo, int out_hi, int op_lo,
-                                   int op_hi, int arg_lo, int arg_hi);
+                                   int op_hi, int arg_lo, int arg_hi, int threads);
 
 template <typename T>
 cudaError_t launch_shuffle_product(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ShuffleKind kind,
                                    TArg<T> out, TArg<T> add, TArg<T> lhs, TArg<T> rhs, int64_t batch, double alpha,
                                    double beta, const ShuffleOrder& ord);
 
+// `op` is the fixed operand, `arg` the cotangent (the kernels' reading order).
 template <typename T>
 cudaError_t launch_shuffle_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ShuffleAdjKind kind,
-                                   TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch, double beta,
-                                   const ShuffleOrder& ord);
+                                   TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch, double beta);
 
 template <typename T>
 cudaError_t launch_pairing(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, T* result, TArg<T> f, TArg<T> a,
@@ -144,7 +144,8 @@ struct PathBatch {
     unsigned int* counter = nullptr;
 };
 
-// `threads` = CTA size of the shared-memory variant (0: heuristic).
+// `threads` = the schedule: CTA size of the shared-memory variant in the low
+// 10 bits (0: heuristic), a cap on CTAs per SM above them (0: none).
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,

@@ -190,10 +190,12 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
                     } else {
                         const uint32_t tail = G.pw[n - 1];
                         const uint32_t a = j / tail, v = j - a * tail;
-                        val = beta * shuffle_word<T, MAXD>(G, n - 1, v, 1, a, L, lhs.lo, lhi, R, rhs.lo, rhi);
+                        val = shuffle_word<T, MAXD>(G, n - 1, v, 1, a, L, lhs.lo, lhi, R, rhs.lo, rhi);
+                        if (beta != T(1)) val *= beta;
                     }
                 } else {
-                    val = beta * shuffle_word<T, MAXD>(G, n, j, 0, 0u, L, lhs.lo, lhi, R, rhs.lo, rhi);
+                    val = shuffle_word<T, MAXD>(G, n, j, 0, 0u, L, lhs.lo, lhi, R, rhs.lo, rhi);
+                    if (beta != T(1)) val *= beta;
                     if (kind == static_cast<int>(ShuffleKind::InplaceFma)) {
                         val = fma(alpha, o[G.db[n] + j], val);
                     } else if (kind == static_cast<int>(ShuffleKind::Fma) && A && add.has(n)) {
@@ -211,32 +213,131 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
 // Adjoints.
 // ---------------------------------------------------------------------------
 
-// Interleaving sum for one output word w (nw letters) and one op degree m:
-//   sum_u OP[ob + u] * ARG[ab + merge(w, u, M)] over the masks M of weight m
-// on nw + m positions (bit b = position b counted from the last letter) and
-// the op words u.  u is split as u_hi W + u_0: a walk over the positions
-// places w's and u_hi's letters, then the inner loop runs over u_0, whose
-// position is the lowest set bit of M.  Lanes [lane0, lane0 + lanes) of a warp
-// share the u_hi range (lanes = 1 for a single thread).
+// The terms of one adjoint coefficient are grouped in items (a, m, M, u_hi):
+// prefix letter a (the left adjoint's letter loop; a single fixed letter or
+// none otherwise), op degree m, interleaving mask M of weight m on the
+// nw + m positions of the merged word (bit b = position b counted from the
+// last letter) and the high part u_hi of the op word u = u_hi W^k + u_lo,
+// k = min(m, 2).  An item sums over the k last letters u_lo:
+//     OP[ob(a, m) + u] * ARG[ab(a, m) + merge(w, u, M)]
+// (W^k terms; one when m = 0), so the walk that places w's and u_hi's
+// letters is paid once per W^k FMAs.  A cursor walks the items in that order; lanes of a
+// warp take every 32nd item, a single thread takes them all.  Skipping ahead
+// costs one Gosper step per mask passed, so each lane pays O(#masks) integer
+// work besides its share of the items.
+struct AdjItems {
+    int kind;
+    int nw;       // letters of the output word w (after the rmul prefix)
+    uint32_t w;   // its index within its degree
+    int a0, a1;   // letter range [a0, a1)
+    int mlo, mhi; // op degree range
+    // cursor
+    int a, m;
+    uint32_t M, last, nhi, uh;
+    bool done;
+
+    __device__ void start_degree(const Geometry& G) {
+        M = (1u << m) - 1u;
+        last = M << nw;
+        nhi = m <= 1 ? 1u : G.pw[m - 2];
+    }
+    __device__ bool next_mask(const Geometry& G) {
+        if (M != last) {
+            const uint32_t low = M & (0u - M);
+            const uint32_t ripple = M + low;
+            M = ripple | (((ripple ^ M) >> 2) >> (__ffs(M) - 1));
+            return true;
+        }
+        if (++m > mhi) {
+            m = mlo;
+            if (++a >= a1) return false;
+        }
+        start_degree(G);
+        return true;
+    }
+    __device__ void init(const Geometry& G, uint32_t first) {
+        a = a0;
+        m = mlo;
+        uh = 0;
+        done = mlo > mhi || a0 >= a1;
+        if (!done) {
+            start_degree(G);
+            advance(G, first);
+        }
+    }
+    __device__ void advance(const Geometry& G, uint32_t k) {
+        uh += k;
+        while (uh >= nhi) {
+            uh -= nhi;
+            if (!next_mask(G)) {
+                done = true;
+                return;
+            }
+        }
+    }
+};
+
 template <typename T>
-__device__ T interleave_sum(const Geometry& G, int nw, uint32_t w, int m, const T* __restrict__ OP, uint32_t ob,
-                            const T* __restrict__ ARG, uint32_t ab, uint32_t first, uint32_t step) {
+__device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const T* __restrict__ OP, int olo,
+                           int ohi, const T* __restrict__ ARG, int alo, int ahi, uint32_t first, uint32_t step) {
     const uint32_t W = static_cast<uint32_t>(G.width);
-    if (m == 0) return first == 0 ? OP[ob] * ARG[ab + w] : T(0);
-    const int N = nw + m;
-    const uint32_t nhi = G.pw[m - 1];
+    AdjItems it;
+    it.kind = kind;
+    if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
+        it.nw = n;
+        it.w = j;
+        it.a0 = 0;
+        it.a1 = static_cast<int>(W);
+        it.mlo = imax(0, imax(olo - 1, alo - 1 - n));
+        it.mhi = imin(ohi - 1, ahi - 1 - n);
+    } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
+        if (n == 0) return T(0);
+        const uint32_t tail = G.pw[n - 1];
+        const uint32_t a = j / tail;
+        it.nw = n - 1;
+        it.w = j - a * tail;
+        it.a0 = static_cast<int>(a);
+        it.a1 = it.a0 + 1;
+        it.mlo = imax(olo, alo - n);
+        it.mhi = imin(ohi, ahi - n);
+    } else {
+        it.nw = n;
+        it.w = j;
+        it.a0 = 0;
+        it.a1 = 1;
+        it.mlo = imax(olo, alo - n);
+        it.mhi = imin(ohi, ahi - n);
+    }
+    it.init(G, first);
     T acc = T(0);
-    uint32_t M = (1u << m) - 1u;
-    const uint32_t last = M << nw;
-    for (;;) {
-        const uint32_t low = M & (0u - M);
-        const uint32_t rest = M & (M - 1u);
-        const uint32_t c0 = G.pw[__ffs(M) - 1];
-        for (uint32_t uh = first; uh < nhi; uh += step) {
-            uint32_t wq = w, uq = uh, base = 0, p = 1;
+    while (!it.done) {
+        const int m = it.m, N = it.nw + m;
+        const uint32_t a = static_cast<uint32_t>(it.a);
+        uint32_t ob, ab;
+        if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
+            ob = G.db[m + 1] + a * G.pw[m];
+            ab = G.db[N + 1] + a * G.pw[N];
+        } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
+            ob = G.db[m];
+            ab = G.db[N + 1] + a * G.pw[N];
+        } else {
+            ob = G.db[m];
+            ab = G.db[N];
+        }
+        if (m == 0) {
+            acc = fma(OP[ob], ARG[ab + it.w], acc);
+        } else {
+            // the k lowest set bits of M carry u_lo; the rest of M carries u_hi
+            const uint32_t M = it.M;
+            const uint32_t b0 = M & (0u - M);
+            const uint32_t r0 = M ^ b0;
+            const uint32_t b1 = m >= 2 ? r0 & (0u - r0) : 0u;
+            const uint32_t rest = r0 ^ b1;
+            const uint32_t c0 = G.pw[__ffs(b0) - 1];
+            uint32_t wq = it.w, uq = it.uh, base = 0, p = 1;
             for (int bpos = 0; bpos < N; ++bpos) {
                 const uint32_t bit = 1u << bpos;
-                if (!(low & bit)) {
+                if (!((b0 | b1) & bit)) {
                     const bool from_u = (rest & bit) != 0;
                     const uint32_t src = from_u ? uq : wq;
                     uint32_t q, r;
@@ -247,64 +348,19 @@ __device__ T interleave_sum(const Geometry& G, int nw, uint32_t w, int m, const 
                 }
                 p *= W;
             }
-            const T* op = OP + ob + uh * W;
-            const T* ar = ARG + ab + base;
-            for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
-        }
-        if (M == last) break;
-        // next mask of the same weight (Gosper)
-        const uint32_t ripple = M + low;
-        M = ripple | (((ripple ^ M) >> 2) >> (__ffs(M) - 1));
-    }
-    return acc;
-}
-
-struct AdjRange {
-    int lo, hi;
-};
-
-// The op-degree range of one output degree n (reference bounds, see the
-// per-kind comments in the file header).
-__device__ __forceinline__ AdjRange adj_range(int kind, int n, int olo, int ohi, int alo, int ahi) {
-    if (kind == static_cast<int>(ShuffleAdjKind::HalfL))
-        return {imax(0, imax(olo - 1, alo - 1 - n)), imin(ohi - 1, ahi - 1 - n)};
-    return {imax(olo, alo - n), imin(ohi, ahi - n)};
-}
-
-template <typename T>
-__device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const T* OP, int olo, int ohi,
-                           const T* ARG, int alo, int ahi, uint32_t first, uint32_t step) {
-    const AdjRange r = adj_range(kind, n, olo, ohi, alo, ahi);
-    T acc = T(0);
-    if (kind == static_cast<int>(ShuffleAdjKind::Shuffle)) {
-        for (int m = r.lo; m <= r.hi; ++m)
-            acc += interleave_sum<T>(G, n, j, m, OP, G.db[m], ARG, G.db[n + m], first, step);
-    } else if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
-        const uint32_t W = static_cast<uint32_t>(G.width);
-        for (int m = r.lo; m <= r.hi; ++m) {
-            // lanes split (letter, u_hi); a thread (step 1) loops over both
-            const uint32_t nhi = m == 0 ? 1u : G.pw[m - 1];
-            for (uint32_t a = 0; a < W; ++a) {
-                // lane slice of this letter's u_hi range in the combined space
-                const uint32_t lo = a * nhi, hi = lo + nhi;
-                uint32_t f = first;
-                if (step > 1) {
-                    if (f < lo) f += ((lo - f + step - 1) / step) * step;
-                    if (f >= hi) continue;
-                } else {
-                    f = lo + first;
-                }
-                acc += interleave_sum<T>(G, n, j, m, OP, G.db[m + 1] + a * G.pw[m], ARG,
-                                         G.db[n + m + 1] + a * G.pw[n + m], f - lo, step);
+            if (m >= 2) {
+                const uint32_t c1 = G.pw[__ffs(b1) - 1];
+                const T* op = OP + ob + it.uh * W * W;
+                const T* ar = ARG + ab + base;
+                for (uint32_t u1 = 0; u1 < W; ++u1, op += W, ar += c1)
+                    for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
+            } else {
+                const T* op = OP + ob;
+                const T* ar = ARG + ab + base;
+                for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
             }
         }
-    } else {
-        if (n == 0) return T(0);
-        const uint32_t tail = G.pw[n - 1];
-        const uint32_t a = j / tail, v = j - a * tail;
-        for (int m = r.lo; m <= r.hi; ++m)
-            acc += interleave_sum<T>(G, n - 1, v, m, OP, G.db[m], ARG, G.db[n + m] + a * G.pw[n - 1 + m], first,
-                                     step);
+        it.advance(G, step);
     }
     return acc;
 }
@@ -344,7 +400,7 @@ __global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, T
                 locate(ord, t, n, j);
                 T acc = adjoint_coeff<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi, lane, 32);
                 acc = warp_reduce(acc);
-                if (lane == 0) o[G.db[n] + j] = beta * acc;
+                if (lane == 0) o[G.db[n] + j] = beta == T(1) ? acc : beta * acc;
             } else {
                 const uint32_t k = nwarp + (t - nwarp) * 32 + lane;
                 if (k < total) {
@@ -352,7 +408,7 @@ __global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, T
                     uint32_t j;
                     locate(ord, k, n, j);
                     const T acc = adjoint_coeff<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi, 0, 1);
-                    o[G.db[n] + j] = beta * acc;
+                    o[G.db[n] + j] = beta == T(1) ? acc : beta * acc;
                 }
             }
         }
@@ -360,7 +416,8 @@ __global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, T
     }
 }
 
-// tensor_pairing: one warp per tensor of the batch.
+// tensor_pairing: one warp per tensor of the batch.  Four independent
+// accumulators keep eight loads per lane in flight (HBM-bound kernel).
 template <typename T>
 __global__ void k_pairing(const T* __restrict__ F, int64_t fs, const T* __restrict__ A, int64_t as, T* result,
                           uint32_t begin, uint32_t end, int64_t batch) {
@@ -370,9 +427,16 @@ __global__ void k_pairing(const T* __restrict__ F, int64_t fs, const T* __restri
          b += warps) {
         const T* f = F + b * fs;
         const T* a = A + b * as;
-        T acc = T(0);
-        for (uint32_t i = begin + lane; i < end; i += 32) acc = fma(f[i], a[i], acc);
-        acc = warp_reduce(acc);
+        T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
+        uint32_t i = begin + lane;
+        for (; i + 96 < end; i += 128) {
+            acc0 = fma(__ldg(f + i), __ldg(a + i), acc0);
+            acc1 = fma(__ldg(f + i + 32), __ldg(a + i + 32), acc1);
+            acc2 = fma(__ldg(f + i + 64), __ldg(a + i + 64), acc2);
+            acc3 = fma(__ldg(f + i + 96), __ldg(a + i + 96), acc3);
+        }
+        for (; i < end; i += 32) acc0 = fma(__ldg(f + i), __ldg(a + i), acc0);
+        T acc = warp_reduce((acc0 + acc1) + (acc2 + acc3));
         if (lane == 0) result[b] = acc;
     }
 }
@@ -408,11 +472,11 @@ ShuffleOrder shuffle_product_order(const Geometry& g, int out_lo, int out_hi) {
 }
 
 ShuffleOrder shuffle_adjoint_order(const Geometry& g, ShuffleAdjKind kind, int out_lo, int out_hi, int op_lo,
-                                   int op_hi, int arg_lo, int arg_hi) {
+                                   int op_hi, int arg_lo, int arg_hi, int threads) {
     // Terms per coefficient of degree n: sum over op degrees m of
-    // C(nw + m, m) W^m (times W for the left adjoint's letter loop).
-    // Coefficients of at least kWarpTerms terms get a warp each.
-    constexpr double kWarpTerms = 1024.0;
+    // C(nw + m, m) W^m (times W for the left adjoint's letter loop).  A
+    // coefficient gets a warp when one thread alone would take more than
+    // twice the CTA's mean work per thread (and at least 128 terms).
     struct Entry {
         int n;
         double cost;
@@ -443,6 +507,9 @@ ShuffleOrder shuffle_adjoint_order(const Geometry& g, ShuffleAdjKind kind, int o
         }
         e[count++] = {n, cost};
     }
+    double total = 0.0;
+    for (int i = 0; i < count; ++i) total += e[i].cost * g.pw[e[i].n];
+    const double kWarpTerms = std::max(128.0, 2.0 * total / std::max(1, threads));
     std::stable_sort(e, e + count, [](const Entry& x, const Entry& y) { return x.cost > y.cost; });
     ShuffleOrder o{};
     uint32_t acc = 0;
@@ -486,9 +553,8 @@ cudaError_t launch_shuffle_product(const Geometry& g, const DeviceInfo& dev, cud
 
 template <typename T>
 cudaError_t launch_shuffle_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ShuffleAdjKind kind,
-                                   TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch, double beta,
-                                   const ShuffleOrder& ord) {
-    if (batch <= 0 || ord.start[ord.count] == 0) return cudaSuccess;
+                                   TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch, double beta) {
+    if (batch <= 0) return cudaSuccess;
     constexpr auto kernel = k_shuffle_adjoint<T>;
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
@@ -497,6 +563,8 @@ cudaError_t launch_shuffle_adjoint(const Geometry& g, const DeviceInfo& dev, cud
     dim3 grid;
     if ((err = shuffle_launch_shape(kernel, g, dev, sizeof(T), batch, threads, smem, staged, grid)) != cudaSuccess)
         return err;
+    const ShuffleOrder ord = shuffle_adjoint_order(g, kind, out.lo, out.hi, op.lo, op.hi, arg.lo, arg.hi, threads);
+    if (ord.start[ord.count] == 0) return cudaSuccess;
     kernel<<<grid, threads, smem, s>>>(g, static_cast<int>(kind), out, op, arg, batch, static_cast<T>(beta), staged,
                                        ord);
     return cudaGetLastError();
@@ -523,8 +591,7 @@ cudaError_t launch_pairing(const Geometry& g, const DeviceInfo& dev, cudaStream_
                                                    TArg<T>, TArg<T>, TArg<T>, TArg<T>, int64_t, double, double,   \
                                                    const ShuffleOrder&);                                          \
     template cudaError_t launch_shuffle_adjoint<T>(const Geometry&, const DeviceInfo&, cudaStream_t,              \
-                                                   ShuffleAdjKind, TArg<T>, TArg<T>, TArg<T>, int64_t, double,    \
-                                                   const ShuffleOrder&);                                          \
+                                                   ShuffleAdjKind, TArg<T>, TArg<T>, TArg<T>, int64_t, double);   \
     template cudaError_t launch_pairing<T>(const Geometry&, const DeviceInfo&, cudaStream_t, T*, TArg<T>, TArg<T>, \
                                            int64_t);
 

@@ -66,6 +66,7 @@ struct SigShared {
     T* Tb;    // scaled cotangent chains
     T* xc;    // two buffers of (D+1)*W: xc[m*W + a] = x_a / m, m = 1..D
     T* inv;   // inv[m] = 1/m
+    T* num;   // num[m] = m (the G update's integer weights, read instead of converted)
     T* part;  // one partial sum per thread
     uint32_t xcs;  // size of one increment buffer
 };
@@ -186,7 +187,7 @@ __device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const
             T* Gi = sh.G + G.db[i];
             for (uint32_t u = threadIdx.x; u < wi; u += blockDim.x) {
                 T s = Gi[u];
-                for (int n = i + 1; n <= D; ++n) s = fma(static_cast<T>(n - i + 1), chain(sg, sh.Tb, n, i)[u], s);
+                for (int n = i + 1; n <= D; ++n) s = fma(sh.num[n - i + 1], chain(sg, sh.Tb, n, i)[u], s);
                 Gi[u] = s;
             }
         }
@@ -311,8 +312,11 @@ __global__ void __launch_bounds__(MAXT) k_signature(SigGeometry sg, const T* __r
     p += 2 * sh.xcs;
     sh.inv = p;
     p += D + 1;
+    sh.num = p;
+    p += D + 2;
     sh.part = p;
     for (int m = threadIdx.x; m <= D; m += blockDim.x) sh.inv[m] = m == 0 ? T(0) : T(1) / static_cast<T>(m);
+    for (int m = threadIdx.x; m <= D + 1; m += blockDim.x) sh.num[m] = static_cast<T>(m);
     __syncthreads();
 
     __shared__ int64_t s_next;
@@ -444,7 +448,7 @@ size_t sig_state_elems(const SigGeometry& sg, bool bwd) {
 template <typename T>
 size_t sig_smem_bytes(const SigGeometry& sg, int threads, bool bwd, bool resident) {
     const size_t D = sg.g.depth, W = sg.g.width;
-    size_t n = 2 * (D + 1) * W + (D + 1) + threads;
+    size_t n = 2 * (D + 1) * W + (D + 1) + (D + 2) + threads;
     if (resident) n += sig_state_elems(sg, bwd);
     return n * sizeof(T);
 }
@@ -454,11 +458,36 @@ size_t sig_smem_bytes(const SigGeometry& sg, int threads, bool bwd, bool residen
 constexpr int kWideThreads = 1024;
 constexpr int kResidentMaxThreads = 512;
 
+// Pad a CTA's dynamic shared memory so that at most `cap` CTAs fit on an SM
+// (fewer, longer waves: 4096 paths over 3 CTAs x 152 SMs is 8.98 waves, over
+// 4 x 152 it is 6.74 and the last wave runs a quarter empty).  Returns false
+// when the cap would not lower the residency.
+template <auto kernel>
+bool cap_residency(const DeviceInfo& dev, int threads, int cap, size_t& smem) {
+    int natural = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&natural, kernel, threads, smem) != cudaSuccess) return false;
+    if (natural <= cap) return false;
+    int per_sm = 0, reserved = 0;
+    cudaFuncAttributes attr{};
+    if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev.device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev.device) != cudaSuccess ||
+        cudaFuncGetAttributes(&attr, kernel) != cudaSuccess)
+        return false;
+    const size_t padded = static_cast<size_t>(per_sm / cap - reserved) - attr.sharedSizeBytes;
+    if (padded < smem || padded + attr.sharedSizeBytes > static_cast<size_t>(dev.max_smem_optin)) return false;
+    smem = padded;
+    return true;
+}
+
+// `schedule` = CTA size in the low 10 bits (0: heuristic) and an optional cap
+// on CTAs per SM above them (0: as many as fit).
 template <typename T, int WT>
 cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStream_t s, const T* incr,
                          PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride, T* grad,
-                         int mode, int threads_req) {
+                         int mode, int schedule) {
     const bool bwd = mode & kBackward;
+    const int threads_req = schedule > 0 ? (schedule & 1023) : 0;
+    const int cap = schedule > 0 ? (schedule >> 10) : 0;
     int threads = threads_req > 0 ? threads_req : threads_for(sg.g.pw[sg.g.depth]);
     if (threads % 32 != 0 || threads > kResidentMaxThreads) return cudaErrorInvalidConfiguration;
     size_t smem = sig_smem_bytes<T>(sg, threads, bwd, true);
@@ -469,6 +498,7 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
         if (err != cudaSuccess) return err;
         // every (degree, letter) pair of the scaled increment needs its own thread
         if (threads < sg.g.depth * sg.g.width || threads < sg.g.width) return cudaErrorInvalidConfiguration;
+        if (cap > 0 && !cap_residency<kernel>(dev, threads, cap, smem)) return cudaErrorInvalidConfiguration;
         dim3 grid;
         if ((err = batch_grid(kernel, dev, threads, smem, paths.batch, grid)) != cudaSuccess) return err;
         kernel<<<grid, threads, smem, s>>>(sg, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, nullptr, 0);
@@ -477,6 +507,7 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
     // State larger than one CTA's shared memory: stream-ordered workspace,
     // one CTA of kWideThreads per SM (the workspace stays within L2 for the
     // shapes of interest), released on the same stream after the launch.
+    if (cap > 0) return cudaErrorInvalidConfiguration;  // one CTA per SM already
     constexpr auto kernel = k_signature<T, 0, kWideThreads>;
     threads = kWideThreads;
     if (threads < sg.g.depth * sg.g.width) return cudaErrorInvalidConfiguration;
