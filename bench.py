@@ -169,11 +169,18 @@ def _time_launches(torch, fn, steps, warmup, stream):
         fn()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nvtx = getattr(torch.cuda, "nvtx", None)
+    try:
+        nvtx.range_push("timed_region")  # lets a profiler select the timed launches
+    except Exception:
+        nvtx = None
     e0.record(stream)
     for _ in range(steps):
         fn()
     e1.record(stream)
     torch.cuda.synchronize()
+    if nvtx is not None:
+        nvtx.range_pop()
     return e0.elapsed_time(e1) / 1e3 / steps
 
 
@@ -323,6 +330,9 @@ def workload_ragged(pkg, torch, args, peak):
 
 
 def workload_fwd_bwd(pkg, torch, args, peak, W, D, B, L, name):
+    if args.batch != BATCH:  # an explicit --batch (profiling captures) replaces the workload's batch
+        B = args.batch
+        name = f"{name.rsplit('_b', 1)[0]}_b{B}"
     basis = pkg.TensorBasis(W, D)
     dim = basis.size()
     st = pkg.GB300Strategy(torch.float64)
@@ -338,7 +348,7 @@ def workload_fwd_bwd(pkg, torch, args, peak, W, D, B, L, name):
         args.steps, args.warmup, torch.cuda.current_stream())
     _line(f"signature fwd+bwd paths/sec (W{W} D{D} L{L} FP64)", B / (ms / 1e3), "paths/s", ms, "f64",
           {"workload": name, "batch": B, "length": L, "threads_per_cta": threads & 1023,
-           "ctas_per_sm_cap": threads >> 10},
+           "ctas_per_sm_cap": (threads >> 10) & 15, "two_launches": bool(threads & (1 << 14))},
           flops=2.0 * 4 * L * step_fma(W, D) * B, peak=peak)
 
 
@@ -478,6 +488,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-operation GPU comparator")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="paths per GPU (default: the headline 4096; smaller only for profiling captures)")
+    ap.add_argument("--schedule", type=int, default=None,
+                    help="pin the signature schedule (rpp_gb_signature_tune's encoding) instead of tuning; "
+                         "for profiling captures")
     ap.add_argument("--workload", default=None,
                     help="other configurations instead of the headline: ft_mul, logsig, ragged, w6d6, w2d12, "
                          "w16d3, adjoints, shuffle or all (comma-separated)")
@@ -520,13 +533,19 @@ def main():
     stream = torch.cuda.current_stream(dev)
     cfg = pkg.DeviceLaunchConfig(stream)
 
-    def step():
-        pkg.signature(strat, cfg, incr, basis, batch, length=LENGTH, out=sig, seed=ell, grad=grad).raise_if_failed()
+    pinned = args.schedule
 
-    # autotune the CTA size on this workload (part of the warm-up)
-    terr, tuned_threads, tuned_ms = pkg.signature_tune(strat, cfg, incr, basis, batch, length=LENGTH, out=sig,
-                                                       seed=ell, grad=grad)
-    terr.raise_if_failed()
+    def step():
+        pkg.signature(strat, cfg, incr, basis, batch, length=LENGTH, out=sig, seed=ell, grad=grad,
+                      schedule=pinned).raise_if_failed()
+
+    if pinned is None:
+        # autotune the schedule on this workload (part of the warm-up)
+        terr, tuned_threads, tuned_ms = pkg.signature_tune(strat, cfg, incr, basis, batch, length=LENGTH, out=sig,
+                                                           seed=ell, grad=grad)
+        terr.raise_if_failed()
+    else:
+        tuned_threads = pinned
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
@@ -538,6 +557,13 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     per_launch = []
     torch.cuda.synchronize()
+    # an NVTX range marks the timed launches (a profiler can select them:
+    # ncu --nvtx --nvtx-include "timed_region/")
+    nvtx = getattr(torch.cuda, "nvtx", None)
+    try:
+        nvtx.range_push("timed_region")
+    except Exception:  # NVTX unavailable: the range is only a profiling aid
+        nvtx = None
     e0.record(stream)
     for _ in range(args.steps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -547,6 +573,8 @@ def main():
         per_launch.append((a, b))
     e1.record(stream)
     torch.cuda.synchronize()
+    if nvtx is not None:
+        nvtx.range_pop()
     clk = clocks.stop()
     elapsed = e0.elapsed_time(e1) / 1e3
     launch_ms = [a.elapsed_time(b) for a, b in per_launch]
@@ -567,7 +595,7 @@ def main():
         incr_d.copy_(incr_p, non_blocking=True)
         ell_d.copy_(ell_p, non_blocking=True)
         pkg.signature(strat, cfg, incr_d, basis, batch, length=LENGTH, out=sig, seed=ell_d,
-                      grad=grad).raise_if_failed()
+                      grad=grad, schedule=pinned).raise_if_failed()
         sig_p.copy_(sig, non_blocking=True)
         grad_p.copy_(grad, non_blocking=True)
 
@@ -643,8 +671,10 @@ def main():
                    "batch_per_gpu": batch, "length": LENGTH, "increments": "N(0,1/256) iid",
                    "seed_functional": "U[-1,1]", "l2": "inputs+outputs 340 MB > L2 (no flush needed)",
                    "kernel": "fused forward+reverse, one launch per step", "parallelism": f"replicas x{world}",
-                   "schedule": {"threads_per_cta": tuned_threads & 1023, "ctas_per_sm_cap": tuned_threads >> 10,
-                                "chosen_by": "rpp_gb_signature_tune"}},
+                   "schedule": {"threads_per_cta": tuned_threads & 1023,
+                                "ctas_per_sm_cap": (tuned_threads >> 10) & 15,
+                                "two_launches": bool(tuned_threads & (1 << 14)),
+                                "chosen_by": "rpp_gb_signature_tune" if pinned is None else "--schedule"}},
         "roofline": {"bound": "fp64_fma", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": (achieved / fp64_peak) if fp64_peak else None, "traffic": None,
                      "peak_source": "measured in-run (rpp_gb_fma_peak, FP64 FMA chains)",
@@ -652,7 +682,8 @@ def main():
                      "fma_per_path": fma_per_path},
         "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps,
+        # signature kernels in the timed region (two per step for the two-launch schedule)
+        "gpu_launches": args.steps * (2 if tuned_threads & (1 << 14) else 1),
         "plain": plain,
         "fused_over_plain": (value / world) / plain["value"] if plain else None,
         "clocks": clk,

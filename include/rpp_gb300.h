@@ -373,18 +373,29 @@ int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream strea
 
 /* Autotuner for rpp_gb_signature (no reference counterpart): runs the same
  * call once per candidate schedule (threads per CTA of the shared-memory
- * kernel, optionally with fewer CTAs per SM than fit, which trades occupancy
- * for a fuller last wave) on the caller's own inputs, times each with CUDA
- * events on `stream`, and records the fastest for this (device, width, depth,
- * dtype, outputs requested, ragged or not); later rpp_gb_signature calls with
- * that key use it.  Synchronises the stream (not capturable); leaves the
- * chosen schedule's outputs in sig/grad.  *threads and *ms (may be NULL)
- * receive the choice and its time per launch: threads per CTA in the low 10
- * bits of *threads, the cap on CTAs per SM (0 = none) above them. */
+ * kernel; optionally fewer CTAs per SM than fit, which trades occupancy for a
+ * fuller last wave; for forward+reverse calls with signature output, also
+ * the same work as a forward launch followed by a reverse launch from the
+ * final signatures, each holding less shared memory per CTA) on the caller's
+ * own inputs, times each with CUDA events on `stream`, and records the
+ * fastest for this (device, width, depth, dtype, outputs requested, ragged or
+ * not); later rpp_gb_signature calls with that key use it.  Synchronises the
+ * stream (not capturable); leaves the chosen schedule's outputs in sig/grad.
+ * *threads and *ms (may be NULL) receive the choice and its time per call:
+ * threads per CTA in bits 0-9 of *threads, the cap on CTAs per SM (0 = none)
+ * in bits 10-13, bit 14 set for the two-launch form. */
 int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
                           const void* incr, const int64_t* offsets, int64_t length, int64_t batch,
                           void* sig, int64_t sig_stride, const void* seed, int64_t seed_stride,
                           void* grad, int32_t* threads, float* ms);
+
+/* rpp_gb_signature under an explicit schedule (encoded as *threads of
+ * rpp_gb_signature_tune), once, without consulting or changing the recorded
+ * choice: for pinning a schedule and for testing every schedule. */
+int rpp_gb_signature_with_schedule(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                                   const void* incr, const int64_t* offsets, int64_t length,
+                                   int64_t batch, void* sig, int64_t sig_stride, const void* seed,
+                                   int64_t seed_stride, void* grad, int32_t schedule);
 
 /* Vector-Jacobian product of exp for a degree-one argument (no reference
  * counterpart; it closes the stored-prefix reverse pass composed from

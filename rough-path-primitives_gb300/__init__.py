@@ -643,7 +643,7 @@ def _ptr(t):
 
 
 def signature(strategy, config, increments, basis, num_batches, *, length=None, offsets=None, out=None,
-              out_stride=None, seed=None, seed_stride=None, grad=None) -> Error:
+              out_stride=None, seed=None, seed_stride=None, grad=None, schedule=None) -> Error:
     """Signatures of piecewise-linear paths in one launch (rpp_gb_signature).
 
     ``increments``: CUDA tensor [total_steps, width]; path b owns rows
@@ -655,11 +655,13 @@ def signature(strategy, config, increments, basis, num_batches, *, length=None, 
     _check_batches(strategy, *(TensorBatch(t, 0, 0, 0) for t in (increments, out, seed, grad) if t is not None))
     dim = basis.size()
     lib = _lib.load()
-    return _status(lib.rpp_gb_signature(
-        basis.plan(strategy.device), _cfg(config).handle(strategy.device), strategy.dtype_code(),
-        _ptr(increments), _ptr(offsets), 0 if length is None else int(length), num_batches, _ptr(out),
-        dim if out_stride is None else out_stride, _ptr(seed), dim if seed_stride is None else seed_stride,
-        _ptr(grad)))
+    args = (basis.plan(strategy.device), _cfg(config).handle(strategy.device), strategy.dtype_code(),
+            _ptr(increments), _ptr(offsets), 0 if length is None else int(length), num_batches, _ptr(out),
+            dim if out_stride is None else out_stride, _ptr(seed), dim if seed_stride is None else seed_stride,
+            _ptr(grad))
+    if schedule is not None:  # an explicit schedule (rpp_gb_signature_with_schedule)
+        return _status(lib.rpp_gb_signature_with_schedule(*args, int(schedule)))
+    return _status(lib.rpp_gb_signature(*args))
 
 
 def exp_letter_vjp(strategy, config, cotangent, x, dx, basis, num_batches, *, cotangent_stride=None,

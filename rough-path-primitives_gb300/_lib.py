@@ -87,6 +87,7 @@ SIGNATURES = {
     "rpp_gb_fma_peak": [_i32, _i32, _DBLP],
     "rpp_gb_signature_tune": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp,
                               ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)],
+    "rpp_gb_signature_with_schedule": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i32],
     "rpp_gb_exp_letter_vjp": [_vp, _vp, _i32, _vp, _i64, _vp, _i64, _vp, _i64, _i64],
 }
 RESTYPES = {"rpp_gb_last_error_string": ctypes.c_char_p, "rpp_gb_version": ctypes.c_char_p}

@@ -347,10 +347,13 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         return rc;
     static const int sizes[] = {128, 192, 256, 320, 384, 512};
     static const int caps[] = {0, 3, 2};
-    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 3];
+    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 4];
     int ncand = 0;
     for (int c : caps)
         for (int t : sizes) candidates[ncand++] = t | (c << 10);
+    // forward + reverse with signature output may also run as two launches
+    if (sig && seed && grad)
+        for (int t : sizes) candidates[ncand++] = t | rpp_gb::kScheduleSplit;
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return fail(RPP_GB_OUT_OF_RESOURCES, "cudaEventCreate failed");
@@ -1064,6 +1067,20 @@ int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t
                                                             sig_stride, seed, seed_stride, grad, threads, ms)
                                    : tune_signature<float>(plan, s, dtype, incr, offsets, length, batch, sig,
                                                            sig_stride, seed, seed_stride, grad, threads, ms);
+    });
+}
+
+int rpp_gb_signature_with_schedule(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* incr,
+                                   const int64_t* offsets, int64_t length, int64_t batch, void* sig,
+                                   int64_t sig_stride, const void* seed, int64_t seed_stride, void* grad,
+                                   int32_t schedule) {
+    if (schedule <= 0) return fail(RPP_GB_INVALID_ARGUMENT, "schedule must be positive");
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_signature<double>(plan, s, dtype, incr, offsets, length, batch, sig,
+                                                           sig_stride, seed, seed_stride, grad, true, schedule)
+                                   : run_signature<float>(plan, s, dtype, incr, offsets, length, batch, sig,
+                                                          sig_stride, seed, seed_stride, grad, true, schedule);
     });
 }
 

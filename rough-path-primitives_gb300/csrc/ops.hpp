@@ -144,8 +144,11 @@ struct PathBatch {
     unsigned int* counter = nullptr;
 };
 
-// `threads` = the schedule: CTA size of the shared-memory variant in the low
-// 10 bits (0: heuristic), a cap on CTAs per SM above them (0: none).
+// `threads` = the schedule: CTA size of the shared-memory variant in bits
+// 0-9 (0: heuristic), a cap on CTAs per SM in bits 10-13 (0: none), and
+// kScheduleSplit: run a forward+reverse call with signature output as a
+// forward launch plus a reverse launch from the final signatures.
+constexpr int kScheduleSplit = 1 << 14;
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,

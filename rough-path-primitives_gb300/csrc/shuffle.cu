@@ -283,11 +283,14 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
     const uint32_t W = static_cast<uint32_t>(G.width);
     AdjItems it;
     it.kind = kind;
+    // the left adjoint's letter loop runs inside each item (a single cursor
+    // pass): an item then holds W times the terms, the m = 0 ones included
+    const uint32_t na = kind == static_cast<int>(ShuffleAdjKind::HalfL) ? W : 1u;
     if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
         it.nw = n;
         it.w = j;
         it.a0 = 0;
-        it.a1 = static_cast<int>(W);
+        it.a1 = 1;
         it.mlo = imax(0, imax(olo - 1, alo - 1 - n));
         it.mhi = imin(ohi - 1, ahi - 1 - n);
     } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
@@ -313,10 +316,13 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
     while (!it.done) {
         const int m = it.m, N = it.nw + m;
         const uint32_t a = static_cast<uint32_t>(it.a);
-        uint32_t ob, ab;
+        // bases of letter 0 and the strides between letters (HalfL only)
+        uint32_t ob, ab, ostep = 0, astep = 0;
         if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
-            ob = G.db[m + 1] + a * G.pw[m];
-            ab = G.db[N + 1] + a * G.pw[N];
+            ob = G.db[m + 1];
+            ab = G.db[N + 1];
+            ostep = G.pw[m];
+            astep = G.pw[N];
         } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
             ob = G.db[m];
             ab = G.db[N + 1] + a * G.pw[N];
@@ -325,7 +331,7 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
             ab = G.db[N];
         }
         if (m == 0) {
-            acc = fma(OP[ob], ARG[ab + it.w], acc);
+            for (uint32_t l = 0; l < na; ++l) acc = fma(OP[ob + l * ostep], ARG[ab + l * astep + it.w], acc);
         } else {
             // the k lowest set bits of M carry u_lo; the rest of M carries u_hi
             const uint32_t M = it.M;
@@ -348,16 +354,18 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
                 }
                 p *= W;
             }
-            if (m >= 2) {
-                const uint32_t c1 = G.pw[__ffs(b1) - 1];
-                const T* op = OP + ob + it.uh * W * W;
-                const T* ar = ARG + ab + base;
-                for (uint32_t u1 = 0; u1 < W; ++u1, op += W, ar += c1)
+            for (uint32_t l = 0; l < na; ++l) {
+                if (m >= 2) {
+                    const uint32_t c1 = G.pw[__ffs(b1) - 1];
+                    const T* op = OP + ob + l * ostep + it.uh * W * W;
+                    const T* ar = ARG + ab + l * astep + base;
+                    for (uint32_t u1 = 0; u1 < W; ++u1, op += W, ar += c1)
+                        for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
+                } else {
+                    const T* op = OP + ob + l * ostep;
+                    const T* ar = ARG + ab + l * astep + base;
                     for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
-            } else {
-                const T* op = OP + ob;
-                const T* ar = ARG + ab + base;
-                for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
+                }
             }
         }
         it.advance(G, step);

@@ -55,7 +55,13 @@ struct SigGeometry {
     uint32_t chain_total;
 };
 
-enum SigMode : int { kForward = 1, kBackward = 2, kLoadFinal = 4, kTopLevel = 8 };
+// kTopGlobal: the top level lives in global memory -- S_D in the output
+// signature row during the forward pass, the seed's top level read from the
+// seed row in the reverse pass -- so a state that misses shared memory by
+// less than one level (W2 D12 FP64: 229 KB, 196 KB without its top) still
+// runs resident.  Level D is only ever updated by the thread that owns the
+// coefficient, so no barrier orders these accesses.
+enum SigMode : int { kForward = 1, kBackward = 2, kLoadFinal = 4, kTopLevel = 8, kTopGlobal = 16 };
 
 template <typename T>
 struct SigShared {
@@ -147,7 +153,7 @@ __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigSha
     const T* x1 = xc + W;
     for (int n = 1; n <= nmax; ++n) {
         const uint32_t wn = G.pw[n];
-        T* Sn = S + G.db[n];
+        T* Sn = n == G.depth ? sh.top : S + G.db[n];
         const T* prev = chain(sg, sh.Tf, n, n - 1);
         for (uint32_t u = threadIdx.x; u < wn; u += blockDim.x) {
             uint32_t q, a;
@@ -276,7 +282,7 @@ __device__ __forceinline__ void backward_step(const SigGeometry& sg, const SigSh
 // memory, L2-resident at the grid sizes used) and only the increments,
 // 1/m and the partials stay in shared memory.
 template <typename T, int WT, int MAXT>
-__global__ void __launch_bounds__(MAXT) k_signature(SigGeometry sg, const T* __restrict__ incr, PathBatch paths,
+__global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? 2 : 1)) k_signature(SigGeometry sg, const T* __restrict__ incr, PathBatch paths,
                                                     T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
                                                     T* grad, int mode, T* gws, int64_t gws_stride) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -287,6 +293,8 @@ __global__ void __launch_bounds__(MAXT) k_signature(SigGeometry sg, const T* __r
     const uint32_t lo = G.db[D];  // coefficients below the top level
     const bool bwd = mode & kBackward;
     const bool fwd_top = mode & kTopLevel;
+    const bool top_global = mode & kTopGlobal;
+    const uint32_t held = top_global ? lo : dim;  // coefficients of S kept on chip
     const int nmax = fwd_top ? D : D - 1;
     const uint32_t slots = blockDim.x / W;
 
@@ -295,7 +303,7 @@ __global__ void __launch_bounds__(MAXT) k_signature(SigGeometry sg, const T* __r
     T* p = gws ? gws + blockIdx.x * gws_stride : q;
     sh.S = p;
     sh.top = p + lo;
-    p += dim;
+    p += held;
     sh.Tf = p;
     p += sg.chain_total;
     if (bwd) {
@@ -337,7 +345,11 @@ __global__ void __launch_bounds__(MAXT) k_signature(SigGeometry sg, const T* __r
             const T* src = sig + b * sig_stride;
             for (uint32_t i = threadIdx.x; i < lo; i += blockDim.x) sh.S[i] = src[i];
         } else {
-            for (uint32_t i = threadIdx.x; i < dim; i += blockDim.x) sh.S[i] = i == 0 ? T(1) : T(0);
+            for (uint32_t i = threadIdx.x; i < held; i += blockDim.x) sh.S[i] = i == 0 ? T(1) : T(0);
+            if (top_global && fwd_top) {
+                sh.top = sig + b * sig_stride + lo;
+                for (uint32_t i = threadIdx.x; i < G.pw[D]; i += blockDim.x) sh.top[i] = T(0);
+            }
         }
 
         if (mode & kForward) {
@@ -351,14 +363,17 @@ __global__ void __launch_bounds__(MAXT) k_signature(SigGeometry sg, const T* __r
             }
             if (sig && !(mode & kLoadFinal)) {
                 T* dst = sig + b * sig_stride;
-                for (uint32_t i = threadIdx.x; i < dim; i += blockDim.x) dst[i] = sh.S[i];
+                for (uint32_t i = threadIdx.x; i < held; i += blockDim.x) dst[i] = sh.S[i];
             }
             __syncthreads();
         }
         if (bwd) {
             const T* sd = seed + b * seed_stride;
             for (uint32_t i = threadIdx.x; i < lo; i += blockDim.x) sh.G[i] = sd[i];
-            for (uint32_t i = threadIdx.x; i < G.pw[D]; i += blockDim.x) sh.top[i] = sd[lo + i];
+            if (top_global)
+                sh.top = const_cast<T*>(sd) + lo;  // read only in the reverse pass
+            else
+                for (uint32_t i = threadIdx.x; i < G.pw[D]; i += blockDim.x) sh.top[i] = sd[lo + i];
             T* gout = grad + off * W;
             if (len > 0) set_increment(sg, sh, xc_buf(sh, len - 1), load_increment(sg, xin, len - 1));
             __syncthreads();
@@ -437,19 +452,20 @@ SigGeometry make_sig_geometry(const Geometry& g) {
     return sg;
 }
 
-// Elements of the state and chain arrays of one CTA.
-size_t sig_state_elems(const SigGeometry& sg, bool bwd) {
-    size_t n = sg.g.dim + sg.chain_total;
+// Elements of the state and chain arrays of one CTA (without the top level
+// when it lives in global memory).
+size_t sig_state_elems(const SigGeometry& sg, bool bwd, bool top_global = false) {
+    size_t n = (top_global ? sg.g.db[sg.g.depth] : sg.g.dim) + sg.chain_total;
     if (bwd) n += sg.g.db[sg.g.depth] + sg.chain_total;
     return n;
 }
 
 // Shared memory of one CTA: the small arrays, plus the state when resident.
 template <typename T>
-size_t sig_smem_bytes(const SigGeometry& sg, int threads, bool bwd, bool resident) {
+size_t sig_smem_bytes(const SigGeometry& sg, int threads, bool bwd, bool resident, bool top_global = false) {
     const size_t D = sg.g.depth, W = sg.g.width;
     size_t n = 2 * (D + 1) * W + (D + 1) + (D + 2) + threads;
-    if (resident) n += sig_state_elems(sg, bwd);
+    if (resident) n += sig_state_elems(sg, bwd, top_global);
     return n * sizeof(T);
 }
 
@@ -487,12 +503,17 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
                          int mode, int schedule) {
     const bool bwd = mode & kBackward;
     const int threads_req = schedule > 0 ? (schedule & 1023) : 0;
-    const int cap = schedule > 0 ? (schedule >> 10) : 0;
+    const int cap = schedule > 0 ? ((schedule >> 10) & 15) : 0;
     int threads = threads_req > 0 ? threads_req : threads_for(sg.g.pw[sg.g.depth]);
     if (threads % 32 != 0 || threads > kResidentMaxThreads) return cudaErrorInvalidConfiguration;
-    size_t smem = sig_smem_bytes<T>(sg, threads, bwd, true);
+    size_t smem = sig_smem_bytes<T>(sg, threads, bwd, true, mode & kTopGlobal);
     // (the kernel also holds a few bytes of static shared memory)
-    if (smem + 64 <= static_cast<size_t>(dev.max_smem_optin)) {
+    const size_t optin = static_cast<size_t>(dev.max_smem_optin);
+    if (smem + 64 > optin && sig_smem_bytes<T>(sg, threads, bwd, true, true) + 64 <= optin) {
+        mode |= kTopGlobal;
+        smem = sig_smem_bytes<T>(sg, threads, bwd, true, true);
+    }
+    if (smem + 64 <= optin) {
         constexpr auto kernel = k_signature<T, WT, kResidentMaxThreads>;
         cudaError_t err = allow_large_smem<kernel>(dev);
         if (err != cudaSuccess) return err;
@@ -524,6 +545,22 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
     return err != cudaSuccess ? err : ferr;
 }
 
+template <typename T>
+cudaError_t launch_width_any(const SigGeometry& sg, const DeviceInfo& dev, cudaStream_t s, const T* incr,
+                             PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride, T* grad,
+                             int mode, int threads) {
+    switch (sg.g.width) {
+        case 2: return launch_width<T, 2>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 3: return launch_width<T, 3>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 4: return launch_width<T, 4>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 5: return launch_width<T, 5>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 6: return launch_width<T, 6>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 8: return launch_width<T, 8>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        case 16: return launch_width<T, 16>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+        default: return launch_width<T, 0>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
+    }
+}
+
 }  // namespace
 
 template <typename T>
@@ -532,6 +569,12 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
                              T* grad, bool forward, int threads) {
     if (paths.batch <= 0) return cudaSuccess;
     const SigGeometry sg = make_sig_geometry(g);
+    // Split schedule: a forward+reverse call with signature output runs as a
+    // forward launch and a reverse launch from the final signatures; the
+    // reverse launch reads the seed's top level from global memory, so both
+    // hold less shared memory per CTA (more CTAs per SM) than the fused one.
+    const bool split = forward && sig && seed && grad && threads > 0 && (threads & kScheduleSplit);
+    if (split) threads &= ~kScheduleSplit;
     int mode = 0;
     if (forward) {
         mode |= kForward;
@@ -558,15 +601,15 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
         }
     }
     cudaError_t err;
-    switch (g.width) {
-        case 2: err = launch_width<T, 2>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
-        case 3: err = launch_width<T, 3>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
-        case 4: err = launch_width<T, 4>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
-        case 5: err = launch_width<T, 5>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
-        case 6: err = launch_width<T, 6>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
-        case 8: err = launch_width<T, 8>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
-        case 16: err = launch_width<T, 16>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
-        default: err = launch_width<T, 0>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads); break;
+    if (split) {
+        err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad,
+                                  kForward | kTopLevel, threads);
+        if (err == cudaSuccess && paths.counter) err = cudaMemsetAsync(paths.counter, 0, sizeof(unsigned int), s);
+        if (err == cudaSuccess)
+            err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad,
+                                      kBackward | kLoadFinal | kTopGlobal, threads);
+    } else {
+        err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
     }
     if (scratch) {
         cudaError_t ferr = cudaFreeAsync(scratch, s);
@@ -631,7 +674,7 @@ cudaError_t launch_signature_static_scratch(const Geometry& g, const DeviceInfo&
     if (sig) mode |= kTopLevel;
     // Only the shared-memory kernel: the global-workspace variant would need an allocation.
     const int t = threads > 0 ? threads : threads_for(g.pw[g.depth]);
-    if (sig_smem_bytes<T>(sg, t, mode & kBackward, true) + 64 > static_cast<size_t>(dev.max_smem_optin)) {
+    if (sig_smem_bytes<T>(sg, t, mode & kBackward, true, true) + 64 > static_cast<size_t>(dev.max_smem_optin)) {
         *refusal = StaticScratchRefusal::StateTooLarge;
         return cudaErrorNotSupported;
     }

@@ -203,9 +203,44 @@ def test_autotuner_records_schedule_and_keeps_parity(orc):
     grad = torch.empty(B * L, W, dtype=torch.float64, device="cuda")
     err, threads, ms = pkg.signature_tune(st, None, dev(incr), basis, B, length=L, out=sig, seed=dev(ell), grad=grad)
     assert err, err.message
-    assert threads in (128, 192, 256, 320, 384, 448, 512) and ms > 0
+    # schedule: threads per CTA in bits 0-9, CTA-per-SM cap in bits 10-13,
+    # bit 14 for the two-launch form
+    assert (threads & 1023) in (128, 192, 256, 320, 384, 512) and ((threads >> 10) & 15) in (0, 2, 3)
+    assert threads < (1 << 15) and ms > 0
     esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
     assert_close(host(sig), esig, TOL_F64, "tuned signature")
     assert_close(host(grad), egrad, TOL_F64, "tuned gradient")
     sig2, grad2 = run(W, D, incr, length=L, ell=ell)
     assert np.array_equal(sig2, host(sig)) or threads != 0
+
+
+@pytest.mark.parametrize("schedule", [128, 256, 128 | (3 << 10), 192 | (2 << 10), 128 | (1 << 14),
+                                      256 | (1 << 14)])
+@pytest.mark.parametrize("ragged", [False, True])
+def test_every_schedule_matches_oracle(orc, schedule, ragged):
+    """Each schedule the autotuner can pick (CTA size, a cap on CTAs per SM,
+    the two-launch form whose reverse launch reads the seed's top level from
+    global memory) gives the oracle's signatures and gradients."""
+    W, D, B, L = 5, 4, 40, 24
+    rng = np.random.default_rng(schedule)
+    lengths = rng.integers(0, 2 * L, B) if ragged else np.full(B, L)
+    offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    incr = rng.normal(0, 1 / np.sqrt(L), (int(offsets[-1]), W))
+    dim = O.tensor_dim(W, D)
+    ell = rng.uniform(-1, 1, (B, dim))
+    basis = pkg.TensorBasis(W, D)
+    sig = torch.full((B, dim), float("nan"), dtype=torch.float64, device="cuda")
+    grad = torch.full((int(offsets[-1]), W), float("nan"), dtype=torch.float64, device="cuda")
+    incr_d, ell_d = dev(incr), dev(ell)
+    off_d = torch.from_numpy(offsets).cuda() if ragged else None
+    lib = pkg.library()
+    rc = lib.rpp_gb_signature_with_schedule(basis.plan(0), torch.cuda.current_stream().cuda_stream, 1,
+                                            incr_d.data_ptr(), None if off_d is None else off_d.data_ptr(),
+                                            0 if ragged else L, B, sig.data_ptr(), dim, ell_d.data_ptr(), dim,
+                                            grad.data_ptr(), schedule)
+    assert rc == 0, lib.rpp_gb_last_error_string()
+    torch.cuda.synchronize()
+    esig, egrad = orc.signature(W, D, incr, offsets, ell=ell)
+    assert_close(host(sig), esig, TOL_F64, f"signature, schedule {schedule}")
+    assert_close(host(grad), egrad, TOL_F64, f"gradient, schedule {schedule}")
+
