@@ -239,8 +239,10 @@ def workload_ft_mul(pkg, torch, args, peak):
 
 
 def workload_logsig(pkg, torch, args, peak):
-    """Log-signatures, W5 D5, 4096 paths of 256 steps: signature, ft_log,
-    tensor_to_lie (one SpMM launch, 829 Lie coefficients, nnz 10 517)."""
+    """Log-signatures, W5 D5, 4096 paths of 256 steps: the signature launch(es)
+    and the fused log-to-Lie epilogue (ft_log + tensor_to_lie in one kernel,
+    829 Lie coefficients, nnz 10 517); the unfused ft_log and tensor_to_lie
+    launches are timed beside it."""
     W, D, B, L = 5, 5, 4096, 256
     basis, lbasis = pkg.TensorBasis(W, D), pkg.LieBasis(W, D)
     dim, ts = basis.size(), lbasis.true_size()
@@ -255,11 +257,12 @@ def workload_logsig(pkg, torch, args, peak):
 
     def run():
         pkg.signature(st, None, incr, basis, B, length=L, out=sig)
-        pkg.ft_log(st, None, full(log), full(sig), basis, B)
-        pkg.tensor_to_lie(st, None, lieb, full(log), lbasis, basis, B, t2l)
+        pkg.tensor_log_to_lie(st, None, lieb, full(sig), lbasis, basis, B, t2l)
 
     stream = torch.cuda.current_stream()
     ms = 1e3 * _time_launches(torch, run, args.steps, args.warmup, stream)
+    ms_fused = 1e3 * _time_launches(torch, lambda: pkg.tensor_log_to_lie(st, None, lieb, full(sig), lbasis, basis,
+                                                                         B, t2l), args.steps, args.warmup, stream)
     log_fma = sum(sum(k * W ** k for k in range(1, m + 1)) for m in range(1, D + 1))
     flops = 2.0 * B * (L * step_fma(W, D) + log_fma + t2l.nnz())
     ms_sig = 1e3 * _time_launches(torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig),
@@ -268,13 +271,48 @@ def workload_logsig(pkg, torch, args, peak):
                                   args.steps, args.warmup, stream)
     ms_t2l = 1e3 * _time_launches(torch, lambda: pkg.tensor_to_lie(st, None, lieb, full(log), lbasis, basis, B, t2l),
                                   args.steps, args.warmup, stream)
-    _line("log-signature paths/sec (W5 D5 L256 FP64): signature + ft_log + tensor_to_lie", B / (ms / 1e3),
-          "paths/s", ms, "f64", {"workload": "logsig_w5_d5_l256_b4096", "launches_per_step": 3},
+    _line("log-signature paths/sec (W5 D5 L256 FP64): signature + fused ft_log/tensor_to_lie", B / (ms / 1e3),
+          "paths/s", ms, "f64", {"workload": "logsig_w5_d5_l256_b4096"},
           flops=flops, peak=peak,
-          extra={"signature_only_ms": ms_sig, "ft_log_ms": ms_log, "tensor_to_lie_ms": ms_t2l,
+          extra={"signature_only_ms": ms_sig, "log_to_lie_fused_ms": ms_fused,
+                 "log_to_lie_fused_roofline_frac": 2.0 * B * (log_fma + t2l.nnz()) / (ms_fused / 1e3) / 1e12 / peak
+                 if peak else None,
+                 "unfused_ft_log_ms": ms_log, "unfused_tensor_to_lie_ms": ms_t2l,
                  "ft_log_roofline_frac": 2.0 * B * log_fma / (ms_log / 1e3) / 1e12 / peak if peak else None,
                  "tensor_to_lie_roofline_frac": 2.0 * B * t2l.nnz() / (ms_t2l / 1e3) / 1e12 / peak
                  if peak else None})
+
+
+def workload_lie_exp(pkg, torch, args, peak):
+    """One log-ODE step per tensor, W5 D5, batch 4096, FP64: out = M (x) exp(l2t(lambda))
+    through the fused kernel, and through lie_to_tensor + ft_fmexp (two launches)
+    for comparison.  lambda ~ U[-0.3, 0.3] on the 828 Lie coefficients."""
+    W, D, B = 5, 5, 4096
+    basis, lbasis = pkg.TensorBasis(W, D), pkg.LieBasis(W, D)
+    dim, ts = basis.size(), lbasis.true_size()
+    st = pkg.GB300Strategy(torch.float64)
+    g = torch.Generator(device="cuda").manual_seed(4)
+    lam = (torch.rand(B, ts, dtype=torch.float64, device="cuda", generator=g) - 0.5) * 0.6
+    mult = torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    out, x = (torch.empty(B, dim, dtype=torch.float64, device="cuda") for _ in range(2))
+    l2t = pkg.make_l2t_matrix(lbasis)
+    full = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
+    lb = pkg.make_lie_batch(lam, ts, 1, D)
+    stream = torch.cuda.current_stream()
+    ms = 1e3 * _time_launches(torch, lambda: pkg.lie_to_tensor_exp(st, None, full(out), full(mult), lb, basis, lbasis,
+                                                                   B, l2t), args.steps, args.warmup, stream)
+
+    def composed():
+        pkg.lie_to_tensor(st, None, full(x), lb, basis, lbasis, B, l2t)
+        pkg.ft_fmexp(st, None, full(out), full(mult), full(x), basis, B)
+
+    ms_c = 1e3 * _time_launches(torch, composed, args.steps, args.warmup, stream)
+    # fmexp: for d = D..1, out = M + out (x) X/d with X truncated to degrees 1..D-d+1
+    fm_fma = sum(min(n, D - d + 1) * W ** n for d in range(1, D + 1) for n in range(1, D + 1))
+    flops = 2.0 * B * (fm_fma + l2t.nnz())
+    _line("Lie-increment exp steps/sec (W5 D5 FP64, batch 4096): fused lie_to_tensor + ft_fmexp",
+          B / (ms / 1e3), "steps/s", ms, "f64", {"workload": "lie_exp_w5_d5_b4096"}, flops=flops, peak=peak,
+          extra={"composed_ms": ms_c, "fused_over_composed": ms_c / ms})
 
 
 def workload_ragged(pkg, torch, args, peak):
@@ -438,7 +476,7 @@ def run_workloads(args):
     peak = _fp64_peak(pkg, 0)
     todo = args.workload.split(",")
     if "all" in todo:
-        todo = ["ft_mul", "logsig", "ragged", "w6d6", "w2d12", "w16d3", "adjoints", "shuffle"]
+        todo = ["ft_mul", "logsig", "lie_exp", "ragged", "w6d6", "w2d12", "w16d3", "adjoints", "shuffle"]
     for w in todo:
         if w == "ft_mul":
             workload_ft_mul(pkg, torch, args, peak)
@@ -452,6 +490,8 @@ def run_workloads(args):
             workload_fwd_bwd(pkg, torch, args, peak, 2, 12, 16384, 64, "fwd_bwd_w2_d12_l64_b16384")
         elif w == "w16d3":
             workload_fwd_bwd(pkg, torch, args, peak, 16, 3, 16384, 64, "fwd_bwd_w16_d3_l64_b16384")
+        elif w == "lie_exp":
+            workload_lie_exp(pkg, torch, args, peak)
         elif w == "shuffle":
             workload_shuffle(pkg, torch, args, peak)
         elif w == "adjoints":
@@ -493,7 +533,7 @@ def main():
                          "for profiling captures")
     ap.add_argument("--workload", default=None,
                     help="other configurations instead of the headline: ft_mul, logsig, ragged, w6d6, w2d12, "
-                         "w16d3, adjoints, shuffle or all (comma-separated)")
+                         "w16d3, adjoints, shuffle, lie_exp or all (comma-separated)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)

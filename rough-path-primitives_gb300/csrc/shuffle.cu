@@ -283,14 +283,11 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
     const uint32_t W = static_cast<uint32_t>(G.width);
     AdjItems it;
     it.kind = kind;
-    // the left adjoint's letter loop runs inside each item (a single cursor
-    // pass): an item then holds W times the terms, the m = 0 ones included
-    const uint32_t na = kind == static_cast<int>(ShuffleAdjKind::HalfL) ? W : 1u;
     if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
         it.nw = n;
         it.w = j;
         it.a0 = 0;
-        it.a1 = 1;
+        it.a1 = static_cast<int>(W);
         it.mlo = imax(0, imax(olo - 1, alo - 1 - n));
         it.mhi = imin(ohi - 1, ahi - 1 - n);
     } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
@@ -316,13 +313,10 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
     while (!it.done) {
         const int m = it.m, N = it.nw + m;
         const uint32_t a = static_cast<uint32_t>(it.a);
-        // bases of letter 0 and the strides between letters (HalfL only)
-        uint32_t ob, ab, ostep = 0, astep = 0;
+        uint32_t ob, ab;
         if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
-            ob = G.db[m + 1];
-            ab = G.db[N + 1];
-            ostep = G.pw[m];
-            astep = G.pw[N];
+            ob = G.db[m + 1] + a * G.pw[m];
+            ab = G.db[N + 1] + a * G.pw[N];
         } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
             ob = G.db[m];
             ab = G.db[N + 1] + a * G.pw[N];
@@ -331,7 +325,7 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
             ab = G.db[N];
         }
         if (m == 0) {
-            for (uint32_t l = 0; l < na; ++l) acc = fma(OP[ob + l * ostep], ARG[ab + l * astep + it.w], acc);
+            acc = fma(OP[ob], ARG[ab + it.w], acc);
         } else {
             // the k lowest set bits of M carry u_lo; the rest of M carries u_hi
             const uint32_t M = it.M;
@@ -354,18 +348,16 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
                 }
                 p *= W;
             }
-            for (uint32_t l = 0; l < na; ++l) {
-                if (m >= 2) {
-                    const uint32_t c1 = G.pw[__ffs(b1) - 1];
-                    const T* op = OP + ob + l * ostep + it.uh * W * W;
-                    const T* ar = ARG + ab + l * astep + base;
-                    for (uint32_t u1 = 0; u1 < W; ++u1, op += W, ar += c1)
-                        for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
-                } else {
-                    const T* op = OP + ob + l * ostep;
-                    const T* ar = ARG + ab + l * astep + base;
+            if (m >= 2) {
+                const uint32_t c1 = G.pw[__ffs(b1) - 1];
+                const T* op = OP + ob + it.uh * W * W;
+                const T* ar = ARG + ab + base;
+                for (uint32_t u1 = 0; u1 < W; ++u1, op += W, ar += c1)
                     for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
-                }
+            } else {
+                const T* op = OP + ob;
+                const T* ar = ARG + ab + base;
+                for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
             }
         }
         it.advance(G, step);
@@ -424,8 +416,7 @@ __global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, T
     }
 }
 
-// tensor_pairing: one warp per tensor of the batch.  Four independent
-// accumulators keep eight loads per lane in flight (HBM-bound kernel).
+// tensor_pairing: one warp per tensor of the batch (HBM-bound).
 template <typename T>
 __global__ void k_pairing(const T* __restrict__ F, int64_t fs, const T* __restrict__ A, int64_t as, T* result,
                           uint32_t begin, uint32_t end, int64_t batch) {
@@ -435,16 +426,9 @@ __global__ void k_pairing(const T* __restrict__ F, int64_t fs, const T* __restri
          b += warps) {
         const T* f = F + b * fs;
         const T* a = A + b * as;
-        T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
-        uint32_t i = begin + lane;
-        for (; i + 96 < end; i += 128) {
-            acc0 = fma(__ldg(f + i), __ldg(a + i), acc0);
-            acc1 = fma(__ldg(f + i + 32), __ldg(a + i + 32), acc1);
-            acc2 = fma(__ldg(f + i + 64), __ldg(a + i + 64), acc2);
-            acc3 = fma(__ldg(f + i + 96), __ldg(a + i + 96), acc3);
-        }
-        for (; i < end; i += 32) acc0 = fma(__ldg(f + i), __ldg(a + i), acc0);
-        T acc = warp_reduce((acc0 + acc1) + (acc2 + acc3));
+        T acc = T(0);
+        for (uint32_t i = begin + lane; i < end; i += 32) acc = fma(f[i], a[i], acc);
+        acc = warp_reduce(acc);
         if (lane == 0) result[b] = acc;
     }
 }
