@@ -132,8 +132,12 @@ __device__ __forceinline__ T warp_sum(T v) {
 // ft_adj_rmul.hpp; semantics as tests/rpp/ft_adjoint_test_helper.hpp:55-87):
 //   left:  out[m][j] = sum_p sum_u op[p][u] arg[m+p][u*W^m + j]
 //   right: out[m][j] = sum_p sum_v op[p][v] arg[m+p][j*W^p + v]
-// Narrow output degrees (fewer coefficients than threads) give each output a
-// warp that splits the sum; wide degrees give each output one thread.
+// Output degrees with fewer coefficients than warps give each coefficient a
+// group of nwarps / W^m warps (the low degrees hold the longest sums: at W16 D3
+// the degree-0 coefficient alone has 4 369 terms); each warp of the group sums
+// every (group*32)-th term and the group's partials are added in warp order
+// after a barrier.  Other narrow degrees (fewer coefficients than threads)
+// give each coefficient a warp; wide degrees give each coefficient a thread.
 template <typename T>
 __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> out, TArg<T> op,
                                                  TArg<T> arg, int64_t batch, int staged) {
@@ -157,7 +161,32 @@ __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> o
         for (int m = out.lo; m <= ohi; ++m) {
             const uint32_t wm = G.pw[m];
             const int pmin = imax(op.lo, arg.lo - m), pmax = imin(phi, ahi - m);
-            if (wm < blockDim.x) {
+            if (wm < static_cast<uint32_t>(nwarps)) {
+                T* s_part = sm + (staged ? 2 * dim : 0);
+                const uint32_t group = static_cast<uint32_t>(nwarps) / wm;
+                const uint32_t j = static_cast<uint32_t>(warp) / group;
+                const uint32_t rank = static_cast<uint32_t>(warp) - j * group;
+                T acc = T(0);
+                if (j < wm) {
+                    const uint32_t step = group * 32;
+                    for (int p = pmin; p <= pmax; ++p) {
+                        const uint32_t wp = G.pw[p];
+                        const T* Pp = P + G.db[p];
+                        const T* Ap = A + G.db[m + p];
+                        for (uint32_t u = rank * 32 + lane; u < wp; u += step)
+                            acc = fma(Pp[u], left ? Ap[u * wm + j] : Ap[j * wp + u], acc);
+                    }
+                }
+                acc = warp_sum(acc);
+                if (lane == 0) s_part[warp] = acc;
+                __syncthreads();
+                if (j < wm && rank == 0 && lane == 0) {
+                    T v = s_part[warp];
+                    for (uint32_t r = 1; r < group; ++r) v += s_part[warp + r];
+                    o[G.db[m] + j] = v;
+                }
+                __syncthreads();
+            } else if (wm < blockDim.x) {
                 for (uint32_t j = warp; j < wm; j += nwarps) {
                     T acc = T(0);
                     for (int p = pmin; p <= pmax; ++p) {
@@ -375,8 +404,9 @@ cudaError_t launch_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
     const size_t smem_need = 2 * static_cast<size_t>(g.dim) * sizeof(T);
-    const int staged = smem_need <= kStageLimit && smem_need <= static_cast<size_t>(dev.max_smem_optin);
-    const size_t smem = staged ? smem_need : 0;
+    const size_t part = 32 * sizeof(T);  // one partial per warp
+    const int staged = smem_need + part <= kStageLimit && smem_need + part <= static_cast<size_t>(dev.max_smem_optin);
+    const size_t smem = (staged ? smem_need : 0) + part;
     const int threads = threads_for(g.pw[g.depth]);
     dim3 grid;
     if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;

@@ -566,6 +566,58 @@ Error<char const*> signature(gpu::strategies::GB300Strategy<Accum, Architecture>
                                                      seed_stride, grad));
 }
 
+// ---- fused steps either side of the signature (no single reference call) ---
+// tensor_log_to_lie: ft_log of `arg` over its own degree range, then
+// tensor_to_lie of that log (include/rpp/operations/intermediate/ft_log.hpp,
+// include/rpp/operations/basic/tensor_to_lie.hpp) in one kernel
+// (rpp_gb_log_to_lie); `out` is a Lie batch.
+template <typename Accum, typename Architecture, typename LieBatch, typename TensorBatch, typename LieBasis,
+          typename TensorBasis, typename Matrix>
+Error<char const*> tensor_log_to_lie(gpu::strategies::GB300Strategy<Accum, Architecture> const& s,
+                                     gpu::DeviceLaunchConfig const& cfg, LieBatch const& out, TensorBatch const& arg,
+                                     LieBasis const& lie_basis, TensorBasis const& tensor_basis,
+                                     typename Architecture::Index n, Matrix const& matrix,
+                                     Accum alpha = Accum{1}) noexcept {
+    rpp_gb_plan const* plan = nullptr;
+    if (auto e = gb300_ops_detail::plan_of(s, tensor_basis, plan); !e) return e;
+    rpp_gb_matrix const* m = nullptr;
+    if (auto e = gpu::strategies::gb300_detail::get_matrix(matrix, s.device_id(), m); !e) return e;
+    auto bases = basis::make_basis_pack(lie_basis, tensor_basis);
+    auto o = gpu::strategies::gb300_detail::vector_arg(out, bases);
+    auto a = gpu::strategies::gb300_detail::tensor_arg(arg, bases);
+    return gb300_ops_detail::status(rpp_gb_log_to_lie(plan, m, cfg.stream,
+                                                      gpu::strategies::gb300_detail::dtype_code<Accum>(), &o, &a,
+                                                      a.min_degree, a.max_degree, static_cast<int64_t>(n),
+                                                      static_cast<double>(alpha)));
+}
+
+// lie_to_tensor_exp: lie_to_tensor of `arg` into out's degree range of a zero
+// tensor X, then out = exp(X) (include/rpp/operations/basic/lie_to_tensor.hpp,
+// include/rpp/operations/intermediate/ft_exp.hpp) in one kernel
+// (rpp_gb_lie_to_tensor_exp); the overload with a multiplier batch computes
+// out = multiplier (x) exp(X) (ft_fmexp.hpp).
+template <typename Accum, typename Architecture, typename TensorBatch, typename LieBatch, typename TensorBasis,
+          typename LieBasis, typename Matrix>
+Error<char const*> lie_to_tensor_exp(gpu::strategies::GB300Strategy<Accum, Architecture> const& s,
+                                     gpu::DeviceLaunchConfig const& cfg, TensorBatch const& out,
+                                     TensorBatch const* multiplier, LieBatch const& arg,
+                                     TensorBasis const& tensor_basis, LieBasis const& lie_basis,
+                                     typename Architecture::Index n, Matrix const& matrix,
+                                     Accum alpha = Accum{1}) noexcept {
+    rpp_gb_plan const* plan = nullptr;
+    if (auto e = gb300_ops_detail::plan_of(s, tensor_basis, plan); !e) return e;
+    rpp_gb_matrix const* m = nullptr;
+    if (auto e = gpu::strategies::gb300_detail::get_matrix(matrix, s.device_id(), m); !e) return e;
+    auto bases = basis::make_basis_pack(tensor_basis, lie_basis);
+    auto o = gpu::strategies::gb300_detail::tensor_arg(out, bases);
+    auto a = gpu::strategies::gb300_detail::vector_arg(arg, bases);
+    rpp_gb_tensor_arg mm{};
+    if (multiplier) mm = gpu::strategies::gb300_detail::tensor_arg(*multiplier, bases);
+    return gb300_ops_detail::status(rpp_gb_lie_to_tensor_exp(
+        plan, m, cfg.stream, gpu::strategies::gb300_detail::dtype_code<Accum>(), &o, multiplier ? &mm : nullptr, &a,
+        o.min_degree, o.max_degree, static_cast<int64_t>(n), static_cast<double>(alpha)));
+}
+
 }  // namespace rpp::ops
 
 #endif  // RPP_GPU_GB300_STRATEGY_HPP

@@ -85,6 +85,24 @@ int rpp_gb_st_inplace_fma(const rpp_gb_plan*, rpp_gb_stream, int32_t t, const rp
                           const rpp_gb_tensor_arg* b, const rpp_gb_tensor_arg* c, int64_t n, double al, double be) {
     head("st_inplace_fma", t, n); rec("a", a); rec("b", b); rec("c", c); tail(al, be); return 0;
 }
+int rpp_gb_log_to_lie(const rpp_gb_plan*, const rpp_gb_matrix*, rpp_gb_stream, int32_t t, const rpp_gb_vector_arg* o,
+                      const rpp_gb_tensor_arg* a, int32_t lo, int32_t hi, int64_t n, double alpha) {
+    head("log_to_lie", t, n);
+    std::snprintf(g_buf, sizeof g_buf, " out{b=%lld,n=%lld} degrees=%d..%d", (long long)o->begin, (long long)o->size,
+                  lo, hi);
+    g_calls += g_buf;
+    rec("arg", a); tail(alpha, 0); return 0;
+}
+int rpp_gb_lie_to_tensor_exp(const rpp_gb_plan*, const rpp_gb_matrix*, rpp_gb_stream, int32_t t,
+                             const rpp_gb_tensor_arg* o, const rpp_gb_tensor_arg* mult, const rpp_gb_vector_arg* a,
+                             int32_t lo, int32_t hi, int64_t n, double alpha) {
+    head("lie_to_tensor_exp", t, n); rec("out", o);
+    if (mult) rec("mult", mult);
+    std::snprintf(g_buf, sizeof g_buf, " arg{b=%lld,n=%lld} degrees=%d..%d", (long long)a->begin, (long long)a->size,
+                  lo, hi);
+    g_calls += g_buf;
+    tail(alpha, 0); return 0;
+}
 int rpp_gb_tensor_pairing(const rpp_gb_plan*, rpp_gb_stream, int32_t t, void* result, const rpp_gb_tensor_arg* f,
                           const rpp_gb_tensor_arg* a, int64_t n) {
     head("tensor_pairing", t, n);

@@ -9,6 +9,7 @@
 #include <rpp/basis/lie_multiplication.hpp>
 #include <rpp/basis/tensor_basis.hpp>
 #include <rpp/gpu/gb300/strategy.hpp>
+#include <rpp/sparse/l2t_matrix.hpp>
 #include <rpp/sparse/t2l_matrix.hpp>
 #include <rpp/views/views.hpp>
 
@@ -64,6 +65,13 @@ int main() {
     bad += !rpp::ops::tensor_to_lie(s, cfg, lie_out, tens_in, lie, basis, 4, m);
     bad += !rpp::ops::tensor_to_lie(s, cfg, lie_out, tens_in, lie, basis, 4, m);  // matrix cached: no new upload
     bad += !rpp::ops::signature(s, cfg, basis, p, static_cast<int64_t const*>(nullptr), 16, 4, p, 121);
+    bad += !rpp::ops::tensor_log_to_lie(s, cfg, lie_out, tens_in, lie, basis, 4, m, 0.5);
+    auto l2t = rpp::sparse::make_l2t_matrix<double>(lie);
+    M ml(l2t.data(), l2t.indices(), l2t.offsets(), l2t.nnz(), l2t.outer_dim(), l2t.inner_dim());
+    auto lie_in = rpp::make_lie_batch(static_cast<double const*>(lbuf.data()), Index{40}, Degree{1}, D);
+    bad += !rpp::ops::lie_to_tensor_exp(s, cfg, full, static_cast<decltype(full) const*>(nullptr), lie_in, basis, lie,
+                                        4, ml);
+    bad += !rpp::ops::lie_to_tensor_exp(s, cfg, full, &full, lie_in, basis, lie, 4, ml, 2.0);
     std::fputs(g_calls.c_str(), stdout);
     std::printf("failures=%d\n", bad);
     return bad;

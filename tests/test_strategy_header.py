@@ -50,7 +50,9 @@ def test_intermediates_and_adjoints(calls):
 
 def test_tensor_to_lie_uses_begin_relative_views_and_caches_matrix(calls):
     uploads = [c for c in calls if c.startswith("matrix_create")]
-    assert uploads == ["matrix_create fmt=1 outer=121 inner=32 nnz=109 dev=2"]
+    # the t2l matrix once (the fused log-to-Lie call reuses it), then the l2t matrix once
+    assert uploads == ["matrix_create fmt=1 outer=121 inner=32 nnz=109 dev=2",
+                       "matrix_create fmt=1 outer=32 inner=121 nnz=133 dev=2"]
     spmv = [c for c in calls if c.startswith("spmv")]
     assert len(spmv) == 2
     assert spmv[0] == "spmv dtype=1 n=4 out{s=40,begin=1,size=32} arg{s=128,begin=0,size=121} a=1 b=0"
@@ -71,3 +73,13 @@ def test_shuffle_algebra(calls):
     assert "left_hs_adj_rmul dtype=1 n=4 out{s=128,1..2} x{s=128,0..4} y{s=121,1..1} a=0 b=2" in calls
     assert "tensor_pairing dtype=1 n=4 result=set f{s=128,1..2} arg{s=121,1..1} a=0 b=0" in calls
 
+
+
+def test_fused_lie_steps(calls):
+    """The C++ helpers for the fused steps pass the views' ranges and the
+    cached matrices (the l2t matrix is uploaded once, like the t2l one)."""
+    assert "log_to_lie dtype=1 n=4 out{b=1,n=32} degrees=0..4 arg{s=128,0..4} a=0.5 b=0" in calls
+    assert "lie_to_tensor_exp dtype=1 n=4 out{s=128,0..4} arg{b=1,n=32} degrees=0..4 a=1 b=0" in calls
+    assert ("lie_to_tensor_exp dtype=1 n=4 out{s=128,0..4} mult{s=128,0..4} arg{b=1,n=32} degrees=0..4 a=2 b=0"
+            in calls)
+    assert sum(c.startswith("matrix_create") for c in calls) == 2
