@@ -347,13 +347,17 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         return rc;
     static const int sizes[] = {128, 192, 256, 320, 384, 512};
     static const int caps[] = {0, 3, 2};
-    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 4];
+    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 5];
     int ncand = 0;
     for (int c : caps)
         for (int t : sizes) candidates[ncand++] = t | (c << 10);
-    // forward + reverse with signature output may also run as two launches
+    // forward + reverse with signature output may also run as two launches,
+    // optionally with the forward launch's top level in global memory
     if (sig && seed && grad)
-        for (int t : sizes) candidates[ncand++] = t | rpp_gb::kScheduleSplit;
+        for (int t : sizes) {
+            candidates[ncand++] = t | rpp_gb::kScheduleSplit;
+            candidates[ncand++] = t | rpp_gb::kScheduleSplit | rpp_gb::kScheduleForwardTopGlobal;
+        }
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return fail(RPP_GB_OUT_OF_RESOURCES, "cudaEventCreate failed");

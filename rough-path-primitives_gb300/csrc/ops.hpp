@@ -147,8 +147,12 @@ struct PathBatch {
 // `threads` = the schedule: CTA size of the shared-memory variant in bits
 // 0-9 (0: heuristic), a cap on CTAs per SM in bits 10-13 (0: none), and
 // kScheduleSplit: run a forward+reverse call with signature output as a
-// forward launch plus a reverse launch from the final signatures.
+// forward launch plus a reverse launch from the final signatures;
+// kScheduleForwardTopGlobal (with kScheduleSplit): the forward launch keeps
+// the top level in the output row in global memory (less shared memory per
+// CTA, more CTAs per SM).
 constexpr int kScheduleSplit = 1 << 14;
+constexpr int kScheduleForwardTopGlobal = 1 << 15;
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,

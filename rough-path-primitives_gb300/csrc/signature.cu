@@ -128,7 +128,7 @@ __device__ __forceinline__ T load_increment(const SigGeometry& sg, const T* path
 // barrier, after which xc_next holds the next step's scaled increment.
 template <typename T, int WT>
 __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigShared<T>& sh, const T* xc,
-                                             T* xc_next, T x_next, int nmax) {
+                                             T* xc_next, T x_next, int nmax, bool top_global) {
     const Geometry& G = sg.g;
     const Width<WT> Wd(G);
     const uint32_t W = Wd.value();
@@ -155,6 +155,30 @@ __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigSha
         const uint32_t wn = G.pw[n];
         T* Sn = n == G.depth ? sh.top : S + G.db[n];
         const T* prev = chain(sg, sh.Tf, n, n - 1);
+        if (n == G.depth && top_global) {
+            // S_D in global memory: four independent read-modify-writes per
+            // batch, so their L2 latencies overlap (each coefficient is owned
+            // by one thread for the whole path)
+            const uint32_t bd = blockDim.x;
+            for (uint32_t u0 = threadIdx.x; u0 < wn; u0 += 4 * bd) {
+                T v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t u = u0 + k * bd;
+                    v[k] = u < wn ? Sn[u] : T(0);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t u = u0 + k * bd;
+                    if (u < wn) {
+                        uint32_t q, a;
+                        Wd.divmod(u, q, a);
+                        Sn[u] = fma(n == 1 ? s0 : prev[q], x1[a], v[k]);
+                    }
+                }
+            }
+            continue;
+        }
         for (uint32_t u = threadIdx.x; u < wn; u += blockDim.x) {
             uint32_t q, a;
             Wd.divmod(u, q, a);
@@ -359,7 +383,7 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? 2 : 1)) k_signature(SigGe
             for (int64_t k = 0; k < len; ++k) {
                 const T x_next = xv;
                 if (k + 2 < len) xv = load_increment(sg, xin, k + 2);
-                forward_step<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k + 1), x_next, nmax);
+                forward_step<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k + 1), x_next, nmax, top_global);
             }
             if (sig && !(mode & kLoadFinal)) {
                 T* dst = sig + b * sig_stride;
@@ -574,7 +598,8 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
     // reverse launch reads the seed's top level from global memory, so both
     // hold less shared memory per CTA (more CTAs per SM) than the fused one.
     const bool split = forward && sig && seed && grad && threads > 0 && (threads & kScheduleSplit);
-    if (split) threads &= ~kScheduleSplit;
+    const bool fwd_top_global = split && (threads & kScheduleForwardTopGlobal);
+    if (split) threads &= ~(kScheduleSplit | kScheduleForwardTopGlobal);
     int mode = 0;
     if (forward) {
         mode |= kForward;
@@ -603,7 +628,7 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
     cudaError_t err;
     if (split) {
         err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad,
-                                  kForward | kTopLevel, threads);
+                                  kForward | kTopLevel | (fwd_top_global ? kTopGlobal : 0), threads);
         if (err == cudaSuccess && paths.counter) err = cudaMemsetAsync(paths.counter, 0, sizeof(unsigned int), s);
         if (err == cudaSuccess)
             err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad,

@@ -206,7 +206,7 @@ def test_autotuner_records_schedule_and_keeps_parity(orc):
     # schedule: threads per CTA in bits 0-9, CTA-per-SM cap in bits 10-13,
     # bit 14 for the two-launch form
     assert (threads & 1023) in (128, 192, 256, 320, 384, 512) and ((threads >> 10) & 15) in (0, 2, 3)
-    assert threads < (1 << 15) and ms > 0
+    assert threads < (1 << 16) and ms > 0
     esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
     assert_close(host(sig), esig, TOL_F64, "tuned signature")
     assert_close(host(grad), egrad, TOL_F64, "tuned gradient")
@@ -215,7 +215,7 @@ def test_autotuner_records_schedule_and_keeps_parity(orc):
 
 
 @pytest.mark.parametrize("schedule", [128, 256, 128 | (3 << 10), 192 | (2 << 10), 128 | (1 << 14),
-                                      256 | (1 << 14)])
+                                      256 | (1 << 14), 128 | (3 << 14), 320 | (3 << 14)])
 @pytest.mark.parametrize("ragged", [False, True])
 def test_every_schedule_matches_oracle(orc, schedule, ragged):
     """Each schedule the autotuner can pick (CTA size, a cap on CTAs per SM,
