@@ -101,6 +101,17 @@ typedef struct rpp_gb_vector_arg {
  * ---------------------------------------------------------------------- */
 int rpp_gb_plan_create(rpp_gb_plan** plan, int32_t width, int32_t depth, int32_t device);
 int rpp_gb_plan_destroy(rpp_gb_plan* plan);
+
+/* Kernels stage operands with bulk copies completing on mbarriers and never
+ * wait on them without a limit: a wait that runs out sets a bit in the plan's
+ * fault word (1 = a bulk-copy wait expired; that launch's results are
+ * invalid) and the kernel returns.  rpp_gb_plan_fault synchronises the plan's
+ * device, returns the word and clears it (no reference counterpart).
+ * rpp_gb_selftest_bounded_wait launches a one-CTA kernel whose wait is made to
+ * expire (a transaction nothing completes, a short limit): afterwards
+ * rpp_gb_plan_fault reports 1. */
+int rpp_gb_plan_fault(const rpp_gb_plan* plan, uint32_t* fault);
+int rpp_gb_selftest_bounded_wait(const rpp_gb_plan* plan, rpp_gb_stream stream);
 const char* rpp_gb_last_error_string(void);
 /* Library version, e.g. "rpp_gb300 1.0.0 sm_103a". */
 const char* rpp_gb_version(void);

@@ -50,6 +50,8 @@ _DBLP = ctypes.POINTER(ctypes.c_double)
 SIGNATURES = {
     "rpp_gb_plan_create": [ctypes.POINTER(_vp), _i32, _i32, _i32],
     "rpp_gb_plan_destroy": [_vp],
+    "rpp_gb_plan_fault": [_vp, ctypes.POINTER(ctypes.c_uint32)],
+    "rpp_gb_selftest_bounded_wait": [_vp, _vp],
     "rpp_gb_last_error_string": [],
     "rpp_gb_version": [],
     "rpp_gb_ft_mul": [_vp, _vp, _i32, _P, _P, _P, _i64, _dbl],

@@ -620,8 +620,24 @@ int rpp_gb_plan_create(rpp_gb_plan** plan, int32_t width, int32_t depth, int32_t
     if ((err = cudaDeviceGetAttribute(&info.max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device)) !=
         cudaSuccess)
         return cuda_status(err, "cudaDeviceGetAttribute");
+    // the fault word kernels report expired bounded waits in
+    uint32_t* fault = nullptr;
+    {
+        DeviceGuard guard(device);
+        if (guard.error() != cudaSuccess) return cuda_status(guard.error(), "cudaSetDevice");
+        if ((err = cudaMalloc(reinterpret_cast<void**>(&fault), sizeof(uint32_t))) != cudaSuccess)
+            return cuda_status(err, "plan fault word");
+        if ((err = cudaMemset(fault, 0, sizeof(uint32_t))) != cudaSuccess) {
+            cudaFree(fault);
+            return cuda_status(err, "plan fault word");
+        }
+    }
+    g.fault = fault;
     auto* p = new (std::nothrow) rpp_gb_plan;
-    if (!p) return fail(RPP_GB_OUT_OF_RESOURCES, "out of host memory");
+    if (!p) {
+        cudaFree(fault);
+        return fail(RPP_GB_OUT_OF_RESOURCES, "out of host memory");
+    }
     p->geometry = g;
     p->device = info;
     *plan = p;
@@ -629,8 +645,29 @@ int rpp_gb_plan_create(rpp_gb_plan** plan, int32_t width, int32_t depth, int32_t
 }
 
 int rpp_gb_plan_destroy(rpp_gb_plan* plan) {
+    if (plan && plan->geometry.fault) {
+        DeviceGuard guard(plan->device.device);
+        cudaFree(plan->geometry.fault);
+    }
     delete plan;
     return ok();
+}
+
+int rpp_gb_plan_fault(const rpp_gb_plan* plan, uint32_t* fault) {
+    if (!plan || !fault) return fail(RPP_GB_INVALID_ARGUMENT, "NULL plan or output");
+    DeviceGuard guard(plan->device.device);
+    if (guard.error() != cudaSuccess) return cuda_status(guard.error(), "cudaSetDevice");
+    cudaError_t err = cudaMemcpy(fault, plan->geometry.fault, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemset(plan->geometry.fault, 0, sizeof(uint32_t));
+    return cuda_status(err, "plan fault word");
+}
+
+int rpp_gb_selftest_bounded_wait(const rpp_gb_plan* plan, rpp_gb_stream stream) {
+    if (!plan) return fail(RPP_GB_INVALID_ARGUMENT, "plan is NULL");
+    DeviceGuard guard(plan->device.device);
+    if (guard.error() != cudaSuccess) return cuda_status(guard.error(), "cudaSetDevice");
+    return cuda_status(rpp_gb::launch_expired_wait(plan->geometry, static_cast<cudaStream_t>(stream)),
+                       "bounded-wait self-test");
 }
 
 int rpp_gb_ft_mul(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const rpp_gb_tensor_arg* out,

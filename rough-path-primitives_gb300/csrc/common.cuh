@@ -53,6 +53,9 @@ struct Geometry {
     uint32_t db[kMaxDepth + 2];
     uint32_t pw[kMaxDepth + 2];
     FastDiv divw;
+    // The plan's fault word (device memory): kernels OR in a code when a
+    // bounded wait runs out (rpp_gb_plan_fault reads and clears it).
+    uint32_t* fault;
 };
 
 // One operand batch as seen by a kernel.

@@ -18,6 +18,7 @@
 // degree search.
 #include <cstdio>
 
+#include "bulk_stage.cuh"
 #include "common.cuh"
 #include "ft_device.cuh"
 #include "launch_util.cuh"
@@ -33,8 +34,11 @@ __global__ void __launch_bounds__(256) k_product(Geometry G, ProductKind kind, T
                                                  TArg<T> x, TArg<T> y, TArg<T> z, int64_t batch,
                                                  T alpha, T beta, int staged) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sm = reinterpret_cast<T*>(smem_raw);
-    const uint32_t dim = G.dim;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* sm = reinterpret_cast<T*>(smem_raw + kBulkHeader);
+    const uint32_t pd = staged_elems<T>(G.dim);
+    uint32_t phase = 0;
+    if (staged) bulk_stage_init(bar);
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         T* dst = out.at(b);
         // The three operand slots, in global memory.
@@ -69,18 +73,13 @@ __global__ void __launch_bounds__(256) k_product(Geometry G, ProductKind kind, T
         if (staged) {
             // Snapshot every operand that is read (old values of an in-place
             // destination included) so the outputs can be written in any order.
-            T* s_add = sm;
-            T* s_l = sm + dim;
-            T* s_r = sm + 2 * dim;
-            if (add.p) stage(s_add, add.p, add.lo, imin(add.hi, G.depth), G);
-            stage(s_l, L.p, L.lo, imin(L.hi, G.depth), G);
-            stage(s_r, R.p, R.lo, imin(R.hi, G.depth), G);
-            __syncthreads();
-            if (add.p) add.p = s_add;
-            L.p = s_l;
-            R.p = s_r;
+            BulkStage<T> st(bar, phase);
+            if (add.p) add.p = st.add(sm, add.p, add.lo, imin(add.hi, G.depth), G);
+            L.p = st.add(sm + pd, L.p, L.lo, imin(L.hi, G.depth), G);
+            R.p = st.add(sm + 2 * pd, R.p, R.lo, imin(R.hi, G.depth), G);
+            if (!st.commit(G.fault)) return;
             product_levels(G, dst, out.lo, imin(out.hi, G.depth), add, alpha, L, R, beta, false);
-            __syncthreads();
+            bulk_stage_reuse();
         } else {
             product_levels(G, dst, out.lo, imin(out.hi, G.depth), add, alpha, L, R, beta, true);
         }
@@ -92,8 +91,11 @@ __global__ void __launch_bounds__(256) k_intermediate(Geometry G, IntermediateKi
                                                       TArg<T> x, TArg<T> m, int64_t batch,
                                                       int staged) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sm = reinterpret_cast<T*>(smem_raw);
-    const uint32_t dim = G.dim;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* sm = reinterpret_cast<T*>(smem_raw + kBulkHeader);
+    const uint32_t pd = staged_elems<T>(G.dim);
+    uint32_t phase = 0;
+    if (staged) bulk_stage_init(bar);
     const int ohi = imin(out.hi, G.depth);
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         Opnd<T> X{x.at(b), imax(1, x.lo), imin(x.hi, G.depth)};
@@ -102,18 +104,15 @@ __global__ void __launch_bounds__(256) k_intermediate(Geometry G, IntermediateKi
         T* o = out.at(b);
         if (staged) {
             T* s_o = sm;
-            T* s_x = sm + dim;
-            T* s_m = sm + 2 * dim;
-            stage(s_x, X.p, X.lo, X.hi, G);
-            if (M.p) stage(s_m, M.p, M.lo, M.hi, G);
-            __syncthreads();
-            X.p = s_x;
-            if (M.p) M.p = s_m;
+            BulkStage<T> st(bar, phase);
+            X.p = st.add(sm + pd, X.p, X.lo, X.hi, G);
+            if (M.p) M.p = st.add(sm + 2 * pd, M.p, M.lo, M.hi, G);
+            if (!st.commit(G.fault)) return;
             intermediate_one(G, kind, s_o, out.lo, ohi, X, M);
             __syncthreads();
             if (out.lo <= ohi)
                 for (uint32_t i = G.db[out.lo] + threadIdx.x; i < G.db[ohi + 1]; i += blockDim.x) o[i] = s_o[i];
-            __syncthreads();
+            bulk_stage_reuse();
         } else {
             intermediate_one(G, kind, o, out.lo, ohi, X, M);
             __syncthreads();
@@ -142,8 +141,11 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> out, TArg<T> op,
                                                  TArg<T> arg, int64_t batch, int staged) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sm = reinterpret_cast<T*>(smem_raw);
-    const uint32_t dim = G.dim;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* sm = reinterpret_cast<T*>(smem_raw + kBulkHeader);
+    const uint32_t pd = staged_elems<T>(G.dim);
+    uint32_t phase = 0;
+    if (staged) bulk_stage_init(bar);
     const int D = G.depth;
     const int ohi = imin(out.hi, D), phi = imin(op.hi, D), ahi = imin(arg.hi, D);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -152,17 +154,16 @@ __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> o
         const T* A = arg.at(b);
         T* o = out.at(b);
         if (staged) {
-            stage(sm, P, op.lo, phi, G);
-            stage(sm + dim, A, arg.lo, ahi, G);
-            __syncthreads();
-            P = sm;
-            A = sm + dim;
+            BulkStage<T> st(bar, phase);
+            P = st.add(sm, P, op.lo, phi, G);
+            A = st.add(sm + pd, A, arg.lo, ahi, G);
+            if (!st.commit(G.fault)) return;
         }
         for (int m = out.lo; m <= ohi; ++m) {
             const uint32_t wm = G.pw[m];
             const int pmin = imax(op.lo, arg.lo - m), pmax = imin(phi, ahi - m);
             if (wm < static_cast<uint32_t>(nwarps)) {
-                T* s_part = sm + (staged ? 2 * dim : 0);
+                T* s_part = sm + (staged ? 2 * pd : 0);
                 const uint32_t group = static_cast<uint32_t>(nwarps) / wm;
                 const uint32_t j = static_cast<uint32_t>(warp) / group;
                 const uint32_t rank = static_cast<uint32_t>(warp) - j * group;
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> o
                 }
             }
         }
-        __syncthreads();
+        bulk_stage_reuse();
     }
 }
 
@@ -367,7 +368,7 @@ cudaError_t launch_product(const Geometry& g, const DeviceInfo& dev, cudaStream_
     constexpr auto kernel = k_product<T>;
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
-    const size_t smem_need = 3 * static_cast<size_t>(g.dim) * sizeof(T);
+    const size_t smem_need = kBulkHeader + 3 * static_cast<size_t>(staged_elems<T>(g.dim)) * sizeof(T);
     const int staged = smem_need <= kStageLimit && smem_need <= static_cast<size_t>(dev.max_smem_optin);
     const size_t smem = staged ? smem_need : 0;
     const int threads = threads_for(g.pw[g.depth]);
@@ -386,7 +387,8 @@ cudaError_t launch_intermediate(const Geometry& g, const DeviceInfo& dev, cudaSt
     constexpr auto kernel = k_intermediate<T>;
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
-    const size_t smem_need = (kind == IntermediateKind::FMExp ? 3 : 2) * static_cast<size_t>(g.dim) * sizeof(T);
+    const size_t smem_need =
+        kBulkHeader + (kind == IntermediateKind::FMExp ? 3 : 2) * static_cast<size_t>(staged_elems<T>(g.dim)) * sizeof(T);
     const int staged = smem_need <= kStageLimit && smem_need <= static_cast<size_t>(dev.max_smem_optin);
     const size_t smem = staged ? smem_need : 0;
     const int threads = threads_for(g.pw[g.depth]);
@@ -403,8 +405,8 @@ cudaError_t launch_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_
     constexpr auto kernel = k_adjoint<T>;
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
-    const size_t smem_need = 2 * static_cast<size_t>(g.dim) * sizeof(T);
-    const size_t part = 32 * sizeof(T);  // one partial per warp
+    const size_t smem_need = 2 * static_cast<size_t>(staged_elems<T>(g.dim)) * sizeof(T);
+    const size_t part = kBulkHeader + 32 * sizeof(T);  // the mbarrier and one partial per warp
     const int staged = smem_need + part <= kStageLimit && smem_need + part <= static_cast<size_t>(dev.max_smem_optin);
     const size_t smem = (staged ? smem_need : 0) + part;
     const int threads = threads_for(g.pw[g.depth]);

@@ -21,6 +21,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "bulk_stage.cuh"
 #include "ft_device.cuh"
 #include "launch_util.cuh"
 #include "ops.hpp"
@@ -61,18 +62,21 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_log_to_lie(Geometry G, CsrDevice m, TArg<T> x, int lo, int hi, T* out,
                                                    int64_t out_stride, int64_t out_size, int64_t batch, T alpha) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* s_x = reinterpret_cast<T*>(smem_raw);
-    T* s_log = s_x + G.dim;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* s_x = reinterpret_cast<T*>(smem_raw + kBulkHeader);
+    T* s_log = s_x + staged_elems<T>(G.dim);
+    uint32_t phase = 0;
+    bulk_stage_init(bar);
     const Opnd<T> none{nullptr, 1, 0};
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         Opnd<T> X{x.at(b), imax(1, x.lo), imin(x.hi, G.depth)};
-        stage(s_x, X.p, X.lo, X.hi, G);
-        __syncthreads();
-        X.p = s_x;
+        BulkStage<T> st(bar, phase);
+        X.p = st.add(s_x, X.p, X.lo, X.hi, G);
+        if (!st.commit(G.fault)) return;
         intermediate_one(G, IntermediateKind::Log, s_log, lo, hi, X, none);
         __syncthreads();
         csr_rows(m, s_log + G.db[lo], out + b * out_stride, out_size, alpha);
-        __syncthreads();
+        bulk_stage_reuse();
     }
 }
 
@@ -80,24 +84,27 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const T* lie, int64_t lie_stride, int lo,
                                                 int hi, TArg<T> out, TArg<T> mult, int64_t batch, T alpha) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* s_x = reinterpret_cast<T*>(smem_raw);
-    T* s_o = s_x + G.dim;  // also holds the Lie vector until X is formed
-    T* s_m = s_o + G.dim;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    const uint32_t pd = staged_elems<T>(G.dim);
+    T* s_x = reinterpret_cast<T*>(smem_raw + kBulkHeader);
+    T* s_o = s_x + pd;  // also holds the Lie vector until X is formed
+    T* s_m = s_o + pd;
+    uint32_t phase = 0;
+    bulk_stage_init(bar);
     const int ohi = imin(out.hi, G.depth);
     const bool fm = mult.p != nullptr;
     const uint32_t view = G.db[hi + 1] - G.db[lo];
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
-        const T* l = lie + b * lie_stride;
-        for (int64_t i = threadIdx.x; i < m.cols_dim; i += blockDim.x) s_o[i] = l[i];
-        for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) s_x[i] = T(0);
+        BulkStage<T> st(bar, phase);
+        const T* l = st.add_span(s_o, lie + b * lie_stride, 0, static_cast<uint32_t>(m.cols_dim));
         Opnd<T> M{nullptr, 1, 0};
         if (fm) {
             M = {mult.at(b), mult.lo, imin(mult.hi, G.depth)};
-            stage(s_m, M.p, M.lo, M.hi, G);
-            M.p = s_m;
+            M.p = st.add(s_m, M.p, M.lo, M.hi, G);
         }
-        __syncthreads();
-        csr_rows(m, s_o, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
+        for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) s_x[i] = T(0);
+        if (!st.commit(G.fault)) return;
+        csr_rows(m, l, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
         __syncthreads();
         const Opnd<T> X{s_x, imax(1, lo), hi};
         intermediate_one(G, fm ? IntermediateKind::FMExp : IntermediateKind::Exp, s_o, out.lo, ohi, X, M);
@@ -105,15 +112,20 @@ __global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const 
         T* o = out.at(b);
         if (out.lo <= ohi)
             for (uint32_t i = G.db[out.lo] + threadIdx.x; i < G.db[ohi + 1]; i += blockDim.x) o[i] = s_o[i];
-        __syncthreads();
+        bulk_stage_reuse();
     }
 }
 
 }  // namespace
 
-size_t log_to_lie_smem(const Geometry& g, size_t elem) { return 2 * static_cast<size_t>(g.dim) * elem; }
+// Staged buffers carry the bulk copy's alignment padding (bulk_stage.cuh).
+static size_t staged_bytes(const Geometry& g, size_t elem) {
+    const size_t per16 = 16 / elem;
+    return (g.dim + 2 * per16 - 1) / per16 * per16 * elem;
+}
+size_t log_to_lie_smem(const Geometry& g, size_t elem) { return kBulkHeader + 2 * staged_bytes(g, elem); }
 size_t lie_exp_smem(const Geometry& g, size_t elem, bool fm) {
-    return (fm ? 3 : 2) * static_cast<size_t>(g.dim) * elem;
+    return kBulkHeader + (fm ? 3 : 2) * staged_bytes(g, elem);
 }
 
 template <typename T>

@@ -132,6 +132,11 @@ cudaError_t launch_lie_exp(const Geometry& g, const DeviceInfo& dev, cudaStream_
                            const T* lie, int64_t lie_stride, int lo, int hi, TArg<T> out, TArg<T> mult,
                            int64_t batch, double alpha);
 
+// Self-test of the bounded mbarrier wait (peak_probe.cu): one CTA waits,
+// with a short limit, for a transaction that nothing completes; the wait
+// expires, the fault word gets kFaultBulkWait and the kernel returns.
+cudaError_t launch_expired_wait(const Geometry& g, cudaStream_t s);
+
 // Fused signature kernels.
 struct PathBatch {
     const int64_t* offsets;  // device, batch + 1 (or nullptr)

@@ -1,12 +1,15 @@
 // peak_probe.cu -- FMA-throughput probe used as the roofline denominator of
 // the FMA-bound kernels (the device's FP64 rate is not a published constant
-// one can trust for a given clock, so the benchmark measures it in-run).
+// one can trust for a given clock, so the benchmark measures it in-run), and
+// the self-test of the bounded mbarrier wait used by the staging helper.
 //
 // Every thread runs 8 independent FMA chains; the grid is 8 CTAs of 256
 // threads per SM, which saturates the FP64 pipes of all four sub-partitions.
 #include <cuda_runtime.h>
 
 #include "../../include/rpp_gb300.h"
+#include "bulk_stage.cuh"
+#include "ops.hpp"
 
 namespace {
 
@@ -64,3 +67,28 @@ extern "C" int rpp_gb_fma_peak(int32_t dtype, int32_t device, double* tflops) {
     cudaSetDevice(prev);
     return err == cudaSuccess ? RPP_GB_SUCCESS : RPP_GB_INTERNAL;
 }
+
+namespace rpp_gb {
+namespace {
+
+// Declares 16 bytes of transaction on an mbarrier and issues no copy, so the
+// phase never completes; the bounded commit must expire (limit 4096 polls),
+// record the fault and return on every thread.
+__global__ void k_expired_wait(uint32_t* fault) {
+    __shared__ __align__(8) uint64_t bar;
+    bulk_stage_init(&bar);
+    uint32_t phase = 0;
+    BulkStage<double> st(&bar, phase);
+    st.bytes = 16;
+    st.commit(fault, 4096);
+}
+
+}  // namespace
+
+cudaError_t launch_expired_wait(const Geometry& g, cudaStream_t s) {
+    k_expired_wait<<<1, 32, 0, s>>>(g.fault);
+    return cudaGetLastError();
+}
+
+}  // namespace rpp_gb
+

@@ -33,6 +33,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "bulk_stage.cuh"
 #include "launch_util.cuh"
 #include "ops.hpp"
 
@@ -44,13 +45,6 @@ __device__ __forceinline__ T warp_reduce(T v) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
     return v;
-}
-
-template <typename T>
-__device__ __forceinline__ void stage_range(T* dst, const T* src, int lo, int hi, const Geometry& G) {
-    if (lo > hi) return;
-    const uint32_t b = G.db[lo], e = G.db[hi + 1];
-    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) dst[i] = src[i];
 }
 
 // Output position k of the visiting order -> (degree, index in degree).
@@ -153,7 +147,11 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
                                                         TArg<T> rhs, int64_t batch, T alpha, T beta, int staged,
                                                         ShuffleOrder ord) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sm = reinterpret_cast<T*>(smem_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* sm = reinterpret_cast<T*>(smem_raw + kBulkHeader);
+    const uint32_t pd = staged_elems<T>(G.dim);
+    uint32_t phase = 0;
+    if (staged) bulk_stage_init(bar);
     __shared__ uint32_t s_next;
     const int e = kind == static_cast<int>(ShuffleKind::LeftHalf) ? 1 : 0;
     const int lhi = imin(lhs.hi, G.depth), rhi = imin(rhs.hi, G.depth);
@@ -167,12 +165,13 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
         const T* A = add.p ? add.at(b) : nullptr;
         if (threadIdx.x == 0) s_next = 0;
         if (staged) {
-            stage_range(sm, L, lhs.lo, lhi, G);
-            stage_range(sm + G.dim, R, rhs.lo, rhi, G);
-            L = sm;
-            R = sm + G.dim;
+            BulkStage<T> st(bar, phase);
+            L = st.add(sm, L, lhs.lo, lhi, G);
+            R = st.add(sm + pd, R, rhs.lo, rhi, G);
+            if (!st.commit(G.fault)) return;
+        } else {
+            __syncthreads();
         }
-        __syncthreads();
         for (;;) {
             uint32_t t = 0;
             if (lane == 0) t = atomicAdd(&s_next, 1u);
@@ -205,7 +204,7 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
                 o[G.db[n] + j] = val;
             }
         }
-        __syncthreads();
+        bulk_stage_reuse();
     }
 }
 
@@ -370,7 +369,11 @@ __global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, T
                                                         TArg<T> arg, int64_t batch, T beta, int staged,
                                                         ShuffleOrder ord) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sm = reinterpret_cast<T*>(smem_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* sm = reinterpret_cast<T*>(smem_raw + kBulkHeader);
+    const uint32_t pd = staged_elems<T>(G.dim);
+    uint32_t phase = 0;
+    if (staged) bulk_stage_init(bar);
     __shared__ uint32_t s_next;
     const int ohi = imin(op.hi, G.depth), ahi = imin(arg.hi, G.depth);
     const uint32_t nwarp = ord.start[ord.warp_entries];
@@ -383,12 +386,13 @@ __global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, T
         T* o = out.at(b);
         if (threadIdx.x == 0) s_next = 0;
         if (staged) {
-            stage_range(sm, P, op.lo, ohi, G);
-            stage_range(sm + G.dim, A, arg.lo, ahi, G);
-            P = sm;
-            A = sm + G.dim;
+            BulkStage<T> st(bar, phase);
+            P = st.add(sm, P, op.lo, ohi, G);
+            A = st.add(sm + pd, A, arg.lo, ahi, G);
+            if (!st.commit(G.fault)) return;
+        } else {
+            __syncthreads();
         }
-        __syncthreads();
         for (;;) {
             uint32_t t = 0;
             if (lane == 0) t = atomicAdd(&s_next, 1u);
@@ -412,7 +416,7 @@ __global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, T
                 }
             }
         }
-        __syncthreads();
+        bulk_stage_reuse();
     }
 }
 
@@ -438,7 +442,8 @@ constexpr size_t kStageLimit = 200 * 1024;
 template <typename Kernel>
 cudaError_t shuffle_launch_shape(Kernel kernel, const Geometry& g, const DeviceInfo& dev, size_t elem, int64_t batch,
                                  int& threads, size_t& smem, int& staged, dim3& grid) {
-    const size_t need = 2 * static_cast<size_t>(g.dim) * elem;
+    const size_t per16 = 16 / elem;  // staged buffers: padded for the bulk copy's alignment shift
+    const size_t need = kBulkHeader + 2 * ((g.dim + 2 * per16 - 1) / per16 * per16) * elem;
     staged = need <= kStageLimit && need <= static_cast<size_t>(dev.max_smem_optin) ? 1 : 0;
     smem = staged ? need : 0;
     threads = threads_for(g.pw[g.depth]);
