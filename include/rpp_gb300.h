@@ -273,6 +273,9 @@ int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_d
                          int64_t inner_dim, int64_t nnz, const int64_t* offsets,
                          const int64_t* indices, const double* values, int32_t device);
 int rpp_gb_matrix_destroy(rpp_gb_matrix* matrix);
+/* The fault word of the sparse products run with this matrix (the same bits
+ * as rpp_gb_plan_fault): synchronises the device, returns and clears it. */
+int rpp_gb_matrix_fault(const rpp_gb_matrix* matrix, uint32_t* fault);
 
 /* rpp::ops::sparse_matrix_vector_product (include/rpp/operations/linalg/
  * sparse_matrix_vector.hpp:57-96) with the CPU strategy's begin-relative

@@ -78,6 +78,7 @@ SIGNATURES = {
     "rpp_gb_tensor_add_identity": [_vp, _vp, _i32, _P, _i64, _dbl],
     "rpp_gb_matrix_create": [ctypes.POINTER(_vp), _i32, _i64, _i64, _i64, _I64P, _I64P, _DBLP, _i32],
     "rpp_gb_matrix_destroy": [_vp],
+    "rpp_gb_matrix_fault": [_vp, ctypes.POINTER(ctypes.c_uint32)],
     "rpp_gb_sparse_matrix_vector": [_vp, _vp, _i32, _V, _V, _i64, _dbl],
     "rpp_gb_log_to_lie": [_vp, _vp, _vp, _i32, _V, _P, _i32, _i32, _i64, _dbl],
     "rpp_gb_lie_to_tensor_exp": [_vp, _vp, _vp, _i32, _P, _P, _V, _i32, _i32, _i64, _dbl],

@@ -884,8 +884,10 @@ int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_d
     const size_t b_col = align(std::max<size_t>(1, rcol.size()) * sizeof(int32_t));
     const size_t b_v64 = align(std::max<size_t>(1, rval.size()) * sizeof(double));
     const size_t b_v32 = align(std::max<size_t>(1, rval32.size()) * sizeof(float));
+    const size_t b_fault = 256;  // the fault word of the SpMM's bounded waits
     char* block = nullptr;
-    if ((err = cudaMalloc(&block, b_off + b_col + b_v64 + b_v32)) != cudaSuccess) return cuda_status(err, "cudaMalloc");
+    if ((err = cudaMalloc(&block, b_off + b_col + b_v64 + b_v32 + b_fault)) != cudaSuccess)
+        return cuda_status(err, "cudaMalloc");
     auto* m = new (std::nothrow) rpp_gb_matrix;
     if (!m) {
         cudaFree(block);
@@ -897,6 +899,12 @@ int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_d
     auto* d_col = reinterpret_cast<int32_t*>(block + b_off);
     auto* d_v64 = reinterpret_cast<double*>(block + b_off + b_col);
     auto* d_v32 = reinterpret_cast<float*>(block + b_off + b_col + b_v64);
+    auto* d_fault = reinterpret_cast<uint32_t*>(block + b_off + b_col + b_v64 + b_v32);
+    if ((err = cudaMemset(d_fault, 0, sizeof(uint32_t))) != cudaSuccess) {
+        cudaFree(block);
+        delete m;
+        return cuda_status(err, "cudaMemset");
+    }
     err = cudaMemcpy(d_off, roff.data(), roff.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
     if (err == cudaSuccess && nnz > 0) err = cudaMemcpy(d_col, rcol.data(), rcol.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
     if (err == cudaSuccess && nnz > 0) err = cudaMemcpy(d_v64, rval.data(), rval.size() * sizeof(double), cudaMemcpyHostToDevice);
@@ -906,7 +914,7 @@ int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_d
         delete m;
         return cuda_status(err, "cudaMemcpy");
     }
-    m->csr = rpp_gb::CsrDevice{d_off, d_col, d_v64, d_v32, rows, cols, nnz, format == RPP_GB_CSC};
+    m->csr = rpp_gb::CsrDevice{d_off, d_col, d_v64, d_v32, rows, cols, nnz, format == RPP_GB_CSC, d_fault};
     *matrix = m;
     return ok();
 }
@@ -975,6 +983,15 @@ int rpp_gb_lie_to_tensor_exp(const rpp_gb_plan* plan, const rpp_gb_matrix* matri
                    ? run_lie_exp<double>(plan, matrix, s, out, multiplier, arg, lo, hi, batch, alpha)
                    : run_lie_exp<float>(plan, matrix, s, out, multiplier, arg, lo, hi, batch, alpha);
     });
+}
+
+int rpp_gb_matrix_fault(const rpp_gb_matrix* matrix, uint32_t* fault) {
+    if (!matrix || !fault) return fail(RPP_GB_INVALID_ARGUMENT, "NULL matrix or output");
+    DeviceGuard guard(matrix->device);
+    if (guard.error() != cudaSuccess) return cuda_status(guard.error(), "cudaSetDevice");
+    cudaError_t err = cudaMemcpy(fault, matrix->csr.fault, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemset(matrix->csr.fault, 0, sizeof(uint32_t));
+    return cuda_status(err, "matrix fault word");
 }
 
 int rpp_gb_lie_basis(int32_t width, int32_t depth, int64_t* true_size, int64_t* degree_begin, int64_t* pairs) {

@@ -65,6 +65,7 @@ struct CsrDevice {
     int64_t cols_dim;
     int64_t nnz;
     bool zero_rest;  // matrix came from CSC: zero the whole out view first
+    uint32_t* fault; // fault word for expired bounded waits (see Geometry::fault)
 };
 
 template <typename T>

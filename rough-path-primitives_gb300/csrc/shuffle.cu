@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
 // Adjoints.
 // ---------------------------------------------------------------------------
 
-// The terms of one adjoint coefficient are grouped in items (a, m, M, u_hi):
+// The terms of one adjoint coefficient are grouped in items (m, a, M, u_hi):
 // prefix letter a (the left adjoint's letter loop; a single fixed letter or
 // none otherwise), op degree m, interleaving mask M of weight m on the
 // nw + m positions of the merged word (bit b = position b counted from the
@@ -220,7 +220,9 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
 // k = min(m, 2).  An item sums over the k last letters u_lo:
 //     OP[ob(a, m) + u] * ARG[ab(a, m) + merge(w, u, M)]
 // (W^k terms; one when m = 0), so the walk that places w's and u_hi's
-// letters is paid once per W^k FMAs.  A cursor walks the items in that order; lanes of a
+// letters is paid once per W^k FMAs.  Items are visited op degree first,
+// highest degree (largest items) first, then letter, mask and u_hi, so that
+// lanes taking every 32nd item get the large items first and balance.  A cursor walks the items in that order; lanes of a
 // warp take every 32nd item, a single thread takes them all.  Skipping ahead
 // costs one Gosper step per mask passed, so each lane pays O(#masks) integer
 // work besides its share of the items.
@@ -247,16 +249,16 @@ struct AdjItems {
             M = ripple | (((ripple ^ M) >> 2) >> (__ffs(M) - 1));
             return true;
         }
-        if (++m > mhi) {
-            m = mlo;
-            if (++a >= a1) return false;
+        if (++a >= a1) {
+            a = a0;
+            if (--m < mlo) return false;
         }
         start_degree(G);
         return true;
     }
     __device__ void init(const Geometry& G, uint32_t first) {
         a = a0;
-        m = mlo;
+        m = mhi;
         uh = 0;
         done = mlo > mhi || a0 >= a1;
         if (!done) {
@@ -364,8 +366,99 @@ __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const
     return acc;
 }
 
+// The same sum for one thread alone: plain nested loops over (a, m, M, u_hi),
+// the cursor's order, without its per-item bookkeeping (most coefficients of
+// high degree hold single-term items).
 template <typename T>
-__global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, TArg<T> out, TArg<T> op,
+__device__ T adjoint_coeff_seq(const Geometry& G, int kind, int n, uint32_t j, const T* __restrict__ OP, int olo,
+                               int ohi, const T* __restrict__ ARG, int alo, int ahi) {
+    const uint32_t W = static_cast<uint32_t>(G.width);
+    int nw = n, a0 = 0, a1 = 1, mlo, mhi;
+    uint32_t w = j;
+    if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
+        a1 = static_cast<int>(W);
+        mlo = imax(0, imax(olo - 1, alo - 1 - n));
+        mhi = imin(ohi - 1, ahi - 1 - n);
+    } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
+        if (n == 0) return T(0);
+        const uint32_t tail = G.pw[n - 1];
+        const uint32_t a = j / tail;
+        nw = n - 1;
+        w = j - a * tail;
+        a0 = static_cast<int>(a);
+        a1 = a0 + 1;
+        mlo = imax(olo, alo - n);
+        mhi = imin(ohi, ahi - n);
+    } else {
+        mlo = imax(olo, alo - n);
+        mhi = imin(ohi, ahi - n);
+    }
+    T acc = T(0);
+    for (int ai = a0; ai < a1; ++ai) {
+        const uint32_t a = static_cast<uint32_t>(ai);
+        for (int m = mlo; m <= mhi; ++m) {
+            const int N = nw + m;
+            uint32_t ob, ab;
+            if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
+                ob = G.db[m + 1] + a * G.pw[m];
+                ab = G.db[N + 1] + a * G.pw[N];
+            } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
+                ob = G.db[m];
+                ab = G.db[N + 1] + a * G.pw[N];
+            } else {
+                ob = G.db[m];
+                ab = G.db[N];
+            }
+            if (m == 0) {
+                acc = fma(OP[ob], ARG[ab + w], acc);
+                continue;
+            }
+            const uint32_t nhi = m <= 1 ? 1u : G.pw[m - 2];
+            uint32_t M = (1u << m) - 1u;
+            const uint32_t last = M << nw;
+            for (;;) {
+                const uint32_t b0 = M & (0u - M);
+                const uint32_t r0 = M ^ b0;
+                const uint32_t b1 = m >= 2 ? r0 & (0u - r0) : 0u;
+                const uint32_t rest = r0 ^ b1;
+                const uint32_t c0 = G.pw[__ffs(b0) - 1];
+                const uint32_t c1 = m >= 2 ? G.pw[__ffs(b1) - 1] : 0u;
+                for (uint32_t uh = 0; uh < nhi; ++uh) {
+                    uint32_t wq = w, uq = uh, base = 0, p = 1;
+                    for (int bpos = 0; bpos < N; ++bpos) {
+                        const uint32_t bit = 1u << bpos;
+                        if (!((b0 | b1) & bit)) {
+                            const bool from_u = (rest & bit) != 0;
+                            const uint32_t src = from_u ? uq : wq;
+                            uint32_t q, r;
+                            G.divw.divmod(src, q, r);
+                            if (from_u) uq = q;
+                            else wq = q;
+                            base += r * p;
+                        }
+                        p *= W;
+                    }
+                    const T* ar = ARG + ab + base;
+                    if (m >= 2) {
+                        const T* op = OP + ob + uh * W * W;
+                        for (uint32_t u1 = 0; u1 < W; ++u1, op += W, ar += c1)
+                            for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
+                    } else {
+                        const T* op = OP + ob;
+                        for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
+                    }
+                }
+                if (M == last) break;
+                const uint32_t ripple = M + b0;
+                M = ripple | (((ripple ^ M) >> 2) >> (__ffs(M) - 1));
+            }
+        }
+    }
+    return acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind, TArg<T> out, TArg<T> op,
                                                         TArg<T> arg, int64_t batch, T beta, int staged,
                                                         ShuffleOrder ord) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -411,7 +504,7 @@ __global__ void __launch_bounds__(256) k_shuffle_adjoint(Geometry G, int kind, T
                     int n;
                     uint32_t j;
                     locate(ord, k, n, j);
-                    const T acc = adjoint_coeff<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi, 0, 1);
+                    const T acc = adjoint_coeff_seq<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi);
                     o[G.db[n] + j] = beta == T(1) ? acc : beta * acc;
                 }
             }

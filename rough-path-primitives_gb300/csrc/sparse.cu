@@ -8,6 +8,7 @@
 // transposed once when the handle is created), each CTA stages one argument
 // vector in shared memory and each thread owns output rows: no atomics, a
 // deterministic summation order, coalesced writes.
+#include "bulk_stage.cuh"
 #include "common.cuh"
 #include "launch_util.cuh"
 #include "ops.hpp"
@@ -31,7 +32,10 @@ __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_s
                                               const T* arg, int64_t arg_stride, int64_t arg_size,
                                               int64_t batch, T alpha, int staged) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* s_arg = reinterpret_cast<T*>(smem_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* s_arg = reinterpret_cast<T*>(smem_raw + kBulkHeader);
+    uint32_t phase = 0;
+    if (staged) bulk_stage_init(bar);
     const T* vals = csr_values<T>(m);
     const int64_t rows = m.rows;
     const int64_t write_end = m.zero_rest ? out_size : rows;
@@ -39,9 +43,9 @@ __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_s
         const T* x = arg + b * arg_stride;
         T* y = out + b * out_stride;
         if (staged) {
-            for (int64_t i = threadIdx.x; i < arg_size; i += blockDim.x) s_arg[i] = x[i];
-            __syncthreads();
-            x = s_arg;
+            BulkStage<T> st(bar, phase);
+            x = st.add_span(s_arg, x, 0, static_cast<uint32_t>(arg_size));
+            if (!st.commit(m.fault)) return;
         }
         for (int64_t r = threadIdx.x; r < write_end; r += blockDim.x) {
             T acc = T(0);
@@ -51,7 +55,7 @@ __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_s
             }
             y[r] = alpha * acc;
         }
-        if (staged) __syncthreads();
+        if (staged) bulk_stage_reuse();
     }
 }
 
@@ -65,8 +69,8 @@ cudaError_t launch_spmm(const CsrDevice& m, const DeviceInfo& dev, cudaStream_t 
     constexpr auto kernel = k_spmm<T>;
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
-    const size_t need = static_cast<size_t>(arg_size) * sizeof(T);
-    const int staged = need <= 96 * 1024;
+    const size_t need = kBulkHeader + static_cast<size_t>(staged_elems<T>(static_cast<uint32_t>(arg_size))) * sizeof(T);
+    const int staged = arg_size < (int64_t{1} << 31) && need <= 96 * 1024;
     const size_t smem = staged ? need : 0;
     const int threads = 256;
     dim3 grid;

@@ -79,3 +79,18 @@ def test_unaligned_rows(orc, stride_pad, offset):
     torch.cuda.synchronize()
     assert_close(out.cpu().numpy(), want, TOL_F64, f"st_adj_mul stride {stride} offset {offset}")
     assert _fault(basis.plan(0)) == 0
+
+
+def test_sparse_fault_word_stays_clear():
+    W, D, B = 4, 4, 16
+    basis, lbasis = pkg.TensorBasis(W, D), pkg.LieBasis(W, D)
+    dim, ts = basis.size(), lbasis.true_size()
+    st = pkg.GB300Strategy(torch.float64)
+    x = torch.rand(B, dim, dtype=torch.float64, device="cuda")
+    lie = torch.empty(B, ts, dtype=torch.float64, device="cuda")
+    t2l = pkg.make_t2l_matrix(lbasis)
+    assert pkg.tensor_to_lie(st, None, pkg.make_lie_batch(lie, ts, 1, D), pkg.make_tensor_batch(x, dim, 0, D),
+                             lbasis, basis, B, t2l)
+    word = ctypes.c_uint32(7)
+    assert pkg.library().rpp_gb_matrix_fault(t2l.handle(0), ctypes.byref(word)) == 0
+    assert word.value == 0
