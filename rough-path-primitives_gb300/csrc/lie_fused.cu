@@ -16,8 +16,9 @@
 // a path given by Lie increments.  X never leaves shared memory.
 //
 // Both kernels hold one tensor of the batch per CTA (grid-stride) and need
-// the work tensors in shared memory; the host composes the unfused kernels
-// for states that do not fit.
+// two work tensors in shared memory (the multiplier of the Lie step is read
+// from global memory); the host composes the unfused kernels for states that
+// do not fit.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -88,7 +89,6 @@ __global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const 
     const uint32_t pd = staged_elems<T>(G.dim);
     T* s_x = reinterpret_cast<T*>(smem_raw + kBulkHeader);
     T* s_o = s_x + pd;  // also holds the Lie vector until X is formed
-    T* s_m = s_o + pd;
     uint32_t phase = 0;
     bulk_stage_init(bar);
     const int ohi = imin(out.hi, G.depth);
@@ -97,11 +97,10 @@ __global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const 
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         BulkStage<T> st(bar, phase);
         const T* l = st.add_span(s_o, lie + b * lie_stride, 0, static_cast<uint32_t>(m.cols_dim));
+        // the multiplier stays in global memory (each coefficient is read once
+        // per Horner round, from L1/L2), so the CTA holds two tensors, not three
         Opnd<T> M{nullptr, 1, 0};
-        if (fm) {
-            M = {mult.at(b), mult.lo, imin(mult.hi, G.depth)};
-            M.p = st.add(s_m, M.p, M.lo, M.hi, G);
-        }
+        if (fm) M = {mult.at(b), mult.lo, imin(mult.hi, G.depth)};
         for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) s_x[i] = T(0);
         if (!st.commit(G.fault)) return;
         csr_rows(m, l, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
@@ -125,7 +124,8 @@ static size_t staged_bytes(const Geometry& g, size_t elem) {
 }
 size_t log_to_lie_smem(const Geometry& g, size_t elem) { return kBulkHeader + 2 * staged_bytes(g, elem); }
 size_t lie_exp_smem(const Geometry& g, size_t elem, bool fm) {
-    return kBulkHeader + (fm ? 3 : 2) * staged_bytes(g, elem);
+    (void)fm;  // the multiplier is read from global memory
+    return kBulkHeader + 2 * staged_bytes(g, elem);
 }
 
 template <typename T>

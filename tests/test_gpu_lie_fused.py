@@ -69,7 +69,8 @@ def test_log_to_lie_matches_oracle_and_composition(orc, W, D, B, dtype):
 
 @pytest.mark.parametrize("W,D,B", SHAPES)
 @pytest.mark.parametrize("with_multiplier", [False, True])
-def test_lie_to_tensor_exp_matches_oracle(orc, W, D, B, with_multiplier):
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_lie_to_tensor_exp_matches_oracle(orc, W, D, B, with_multiplier, dtype):
     basis, lbasis, dim, ts = _setup(W, D)
     rng = np.random.default_rng(W * 7 + D)
     lam = rng.uniform(-0.5, 0.5, (B, ts))
@@ -84,16 +85,17 @@ def test_lie_to_tensor_exp_matches_oracle(orc, W, D, B, with_multiplier):
         orc.ft_fmexp(W, D, want, mult, X, ((0, D), (0, D), (0, D)))
     else:
         orc.ft_exp(W, D, want, X, ((0, D), (0, D)))
-    st = pkg.GB300Strategy(torch.float64)
-    lamd = torch.from_numpy(lam).cuda()
-    out = torch.full((B, dim), float("nan"), dtype=torch.float64, device="cuda")
+    st = pkg.GB300Strategy(dtype)
+    lamd = torch.from_numpy(lam).to("cuda", dtype)
+    out = torch.full((B, dim), float("nan"), dtype=dtype, device="cuda")
     l2t = pkg.make_l2t_matrix(lbasis)
     full = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
-    mb = full(torch.from_numpy(mult).cuda()) if with_multiplier else None
+    mb = full(torch.from_numpy(mult).to("cuda", dtype)) if with_multiplier else None
     assert pkg.lie_to_tensor_exp(st, None, full(out), mb, pkg.make_lie_batch(lamd, ts, 1, D), basis, lbasis, B,
                                  l2t, alpha=0.75)
     torch.cuda.synchronize()
-    assert_close(out.cpu().numpy(), want, TOL_F64, f"lie_to_tensor_exp W{W} D{D} mult={with_multiplier}")
+    tol = TOL_F64 if dtype == torch.float64 else TOL_F32
+    assert_close(out.double().cpu().numpy(), want, tol, f"lie_to_tensor_exp W{W} D{D} mult={with_multiplier}")
 
 
 def test_partial_views_and_errors():
