@@ -123,6 +123,34 @@ __device__ __forceinline__ T load_increment(const SigGeometry& sg, const T* path
     return T(0);
 }
 
+// Row mode (reverse pass).  A level-j array splits into W^{j-1} rows of W
+// consecutive coefficients (prefix word, then the last letter), and every
+// chain link multiplies a row by one prefix coefficient.  With W fixed at
+// compile time one thread takes a whole row: W FMAs per prefix coefficient
+// loaded, with no index split per coefficient.
+//  * Phase B (kRowModeB): the cotangent chains of one stage form one run of
+//    rows, offsets carried from chain to chain so warps stay full, with the
+//    scaled increment in registers.
+//  * Phase A (kRowModeA): the recovery of S_j and of the chain links T^n_j
+//    row by row, in stages with at least kRowMin rows (a warp instruction
+//    occupies the FP64 pipe for the same time however few of its lanes are
+//    active, so smaller stages keep one thread per coefficient).  Rows are
+//    W elements apart, so W = 4 and 8 (4- and 8-way shared-memory bank
+//    conflicts on 8-byte rows) keep one thread per coefficient too.
+// The forward step keeps one thread per coefficient: measured on W5 D5 and
+// W2 D12, row mode there was slower.
+template <int WT>
+constexpr bool kRowModeB = WT > 0 && WT <= 8;
+template <int WT>
+constexpr bool kRowModeA = WT == 2 || WT == 3 || WT == 5 || WT == 6 || WT == 7;
+constexpr uint32_t kRowMin = 32;
+
+template <typename T, int WT>
+__device__ __forceinline__ void load_row(T (&r)[WT], const T* src) {
+#pragma unroll
+    for (int a = 0; a < WT; ++a) r[a] = src[a];
+}
+
 // One forward step S <- S (x) exp(x).  `nmax` = D when the top level is
 // maintained, D-1 when it is not needed (gradient-only calls).  Ends with a
 // barrier, after which xc_next holds the next step's scaled increment.
@@ -190,13 +218,36 @@ __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigSha
     __syncthreads();
 }
 
+// Partial letter gradients of one reverse step.  Thread t accumulated letter
+// t mod W; lanes of a warp with the same letter (lanes l, l + W, l + 2W, ...)
+// are summed by a shuffle tree, and lane l < W of warp w stores the warp's
+// partial of letter (32w + l) mod W at part[w*W + letter] -- log2(32/W) adds
+// per warp instead of W threads each adding blockDim/W partials in sequence.
+// W > 16 keeps one partial per thread (part[t]).  partial_groups() gives the
+// number of partials per letter either way.
+template <typename T>
+__device__ __forceinline__ void store_partials(const SigShared<T>& sh, T v, uint32_t W) {
+    if (W > 16) {
+        sh.part[threadIdx.x] = v;
+        return;
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t off = W; off < 32u; off *= 2u) {
+        const T o = __shfl_down_sync(0xffffffffu, v, off);
+        if (lane + off < 32u) v += o;
+    }
+    if (lane < W) sh.part[(threadIdx.x >> 5) * W + threadIdx.x % W] = v;
+}
+
+__device__ __forceinline__ uint32_t partial_groups(uint32_t W) { return W > 16 ? blockDim.x / W : blockDim.x / 32; }
+
 // Finish a reverse step: grad_k from the partials (the stage-1 terms
 // sum_n Gh^n_1[a] S_0 folded in) and, when `update_g`, G_{k-1} from the
 // cotangent chains.  Runs between barriers; thread a < W reads G_1[a] before it
 // updates that same element (level-1 element u is updated by thread u).
 template <typename T>
 __device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const SigShared<T>& sh, T* grad_k,
-                                                    bool update_g, uint32_t slots) {
+                                                    bool update_g, uint32_t groups) {
     const Geometry& G = sg.g;
     const int D = G.depth;
     const uint32_t W = static_cast<uint32_t>(G.width);
@@ -208,7 +259,7 @@ __device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const
             const T* g1 = n == 1 ? (D == 1 ? sh.top : sh.G + G.db[1]) : chain(sg, sh.Tb, n, 1);
             v = fma(g1[a], s0, v);
         }
-        for (uint32_t s = 0; s < slots; ++s) v += sh.part[s * W + a];
+        for (uint32_t s = 0; s < groups; ++s) v += sh.part[s * W + a];
         grad_k[a] = v;
     }
     if (update_g) {
@@ -244,14 +295,38 @@ __device__ __forceinline__ void backward_step(const SigGeometry& sg, const SigSh
 
     // Phase A: recover S_1..S_{D-1} of the prefix and the forward chains.
     if (D == 1 && pending_grad) {
-        finish_reverse_step(sg, sh, pending_grad, true, slots);
+        finish_reverse_step(sg, sh, pending_grad, true, partial_groups(W));
         __syncthreads();
     }
     for (int j = 1; j < D; ++j) {
-        if (j == 1 && pending_grad) finish_reverse_step(sg, sh, pending_grad, true, slots);
+        if (j == 1 && pending_grad) finish_reverse_step(sg, sh, pending_grad, true, partial_groups(W));
         const uint32_t wj = G.pw[j];
         T* Sj = S + G.db[j];
         const T* own = chain(sg, sh.Tf, j, j - 1);
+        if constexpr (kRowModeA<WT>) {
+            const uint32_t rows = G.pw[j - 1];
+            if (rows >= kRowMin) {  // (so j >= 2 and every prefix comes from a chain)
+                for (uint32_t q = threadIdx.x; q < rows; q += blockDim.x) {
+                    const T o = own[q];
+                    T* Sq = Sj + q * WT;
+                    T s[WT];
+#pragma unroll
+                    for (int a = 0; a < WT; ++a) {
+                        s[a] = fma(-o, x1[a], Sq[a]);
+                        Sq[a] = s[a];
+                    }
+                    for (int n = j + 1; n <= D; ++n) {
+                        const T p = chain(sg, sh.Tf, n, j - 1)[q];
+                        const T* xm = xc + (n - j + 1) * WT;
+                        T* dst = chain(sg, sh.Tf, n, j) + q * WT;
+#pragma unroll
+                        for (int a = 0; a < WT; ++a) dst[a] = fma(p, xm[a], s[a]);
+                    }
+                }
+                __syncthreads();
+                continue;
+            }
+        }
         for (uint32_t u = threadIdx.x; u < wj; u += blockDim.x) {
             uint32_t q, a;
             Wd.divmod(u, q, a);
@@ -270,7 +345,28 @@ __device__ __forceinline__ void backward_step(const SigGeometry& sg, const SigSh
     T xacc = T(0);
     for (int j = D; j >= 2; --j) {
         const uint32_t wjm1 = G.pw[j - 1];
-        for (int n = j; n <= D; ++n) {
+        if constexpr (kRowModeB<WT>) {
+            // the chains of this stage as one run of rows (offsets carried
+            // across chains), the scaled increment in registers
+            uint32_t r = threadIdx.x;
+            for (int n = j; n <= D; ++n) {
+                if (r < wjm1) {
+                    const T* gin = n == j ? (j == D ? sh.top : sh.G + G.db[j]) : chain(sg, sh.Tb, n, j);
+                    T* gout = chain(sg, sh.Tb, n, j - 1);
+                    T x[WT];
+                    load_row(x, xc + (n - j + 2) * WT);
+                    for (; r < wjm1; r += blockDim.x) {
+                        const T* row = gin + r * WT;
+                        T acc = T(0);
+#pragma unroll
+                        for (int a = 0; a < WT; ++a) acc = fma(row[a], x[a], acc);
+                        gout[r] = acc;
+                    }
+                }
+                r -= wjm1;
+            }
+        }
+        for (int n = j; n <= D && !kRowModeB<WT>; ++n) {
             const T* gin = n == j ? (j == D ? sh.top : sh.G + G.db[j]) : chain(sg, sh.Tb, n, j);
             T* gout = chain(sg, sh.Tb, n, j - 1);
             const T* xm = xc + (n - j + 2) * W;
@@ -287,16 +383,19 @@ __device__ __forceinline__ void backward_step(const SigGeometry& sg, const SigSh
             }
         }
         if (xbar_lane) {
+            // rows of all chains of the stage in one run (offsets carried)
+            uint32_t u = my_slot;
             for (int n = j; n <= D; ++n) {
                 const T* gin = n == j ? (j == D ? sh.top : sh.G + G.db[j]) : chain(sg, sh.Tb, n, j);
                 const T* tprev = chain(sg, sh.Tf, n, j - 1);
 #pragma unroll 4
-                for (uint32_t u = my_slot; u < wjm1; u += slots) xacc = fma(gin[u * W + my_a], tprev[u], xacc);
+                for (; u < wjm1; u += slots) xacc = fma(gin[u * W + my_a], tprev[u], xacc);
+                u -= wjm1;
             }
         }
         __syncthreads();
     }
-    sh.part[threadIdx.x] = xbar_lane ? xacc : T(0);
+    store_partials(sh, xbar_lane ? xacc : T(0), W);
     set_increment(sg, sh, xc_next, x_next);
     __syncthreads();
 }
@@ -320,7 +419,6 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? 2 : 1)) k_signature(SigGe
     const bool top_global = mode & kTopGlobal;
     const uint32_t held = top_global ? lo : dim;  // coefficients of S kept on chip
     const int nmax = fwd_top ? D : D - 1;
-    const uint32_t slots = blockDim.x / W;
 
     SigShared<T> sh;
     T* q = reinterpret_cast<T*>(smem_raw);
@@ -409,7 +507,7 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? 2 : 1)) k_signature(SigGe
                                      k + 1 < len ? gout + (k + 1) * W : nullptr);
             }
             if (len > 0) {
-                finish_reverse_step(sg, sh, gout, false, slots);
+                finish_reverse_step(sg, sh, gout, false, partial_groups(W));
                 __syncthreads();
             }
         }
