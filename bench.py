@@ -33,6 +33,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WIDTH, DEPTH, BATCH, LENGTH = 5, 5, 4096, 256
+# DRAM bytes of one headline step under the two-launch schedule, from a
+# one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, nine steps)
+# of `python bench.py --steps 2 --warmup 3 --no-cpu-baseline --no-plain
+# --schedule 16512`: forward launch 42.8 MB read + 65.5 MB written, reverse
+# launch 199.0 MB read + 28.0 MB written: the compulsory inputs and outputs,
+# with the seed's top level re-read from L2, not DRAM.
+TWO_LAUNCH_TRAFFIC_BYTES = 335.3e6
 METRIC = "signature fwd+bwd paths/sec (d=5,N=5,L=256) fused vs plain; % of roofline"
 
 
@@ -728,14 +735,19 @@ def main():
         "config": {"workload": "signature_fwd_bwd_w5_d5_l256", "width": WIDTH, "depth": DEPTH,
                    "batch_per_gpu": batch, "length": LENGTH, "increments": "N(0,1/256) iid",
                    "seed_functional": "U[-1,1]", "l2": "inputs+outputs 340 MB > L2 (no flush needed)",
-                   "kernel": "fused forward+reverse, one launch per step", "parallelism": f"replicas x{world}",
+                   "kernel": ("fused forward+reverse: a forward launch and a reverse launch per step"
+                              if tuned_threads & (1 << 14) else "fused forward+reverse, one launch per step"),
+                   "parallelism": f"replicas x{world}",
                    "schedule": {"threads_per_cta": tuned_threads & 1023,
                                 "ctas_per_sm_cap": (tuned_threads >> 10) & 15,
                                 "two_launches": bool(tuned_threads & (1 << 14)),
                                 "forward_top_level_in_global": bool(tuned_threads & (1 << 15)),
+                                "reverse_threads_per_cta": ((tuned_threads >> 16) & 1023) or (tuned_threads & 1023),
                                 "chosen_by": "rpp_gb_signature_tune" if pinned is None else "--schedule"}},
         "roofline": {"bound": "fp64_fma", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": (achieved / fp64_peak) if fp64_peak else None, "traffic": None,
+                     "frac": (achieved / fp64_peak) if fp64_peak else None,
+                     "traffic": TWO_LAUNCH_TRAFFIC_BYTES if tuned_threads & (1 << 14) else None,
+                     "traffic_unit": "DRAM bytes per step (both launches), ncu capture of the two-launch schedule",
                      "peak_source": "measured in-run (rpp_gb_fma_peak, FP64 FMA chains)",
                      "algorithmic_flops_per_launch": flops_per_launch,
                      "fma_per_path": fma_per_path},

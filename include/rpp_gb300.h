@@ -398,7 +398,10 @@ int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream strea
  * *threads and *ms (may be NULL) receive the choice and its time per call:
  * threads per CTA in bits 0-9 of *threads, the cap on CTAs per SM (0 = none)
  * in bits 10-13, bit 14 set for the two-launch form, bit 15 set when its
- * forward launch keeps the top level in the output row in global memory. */
+ * forward launch keeps the top level in the output row in global memory, and
+ * for the two-launch form the reverse launch's own CTA size in bits 16-25
+ * (0: the same as the forward launch's).  A two-launch winner is refined by
+ * timing other reverse sizes, then other forward sizes. */
 int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
                           const void* incr, const int64_t* offsets, int64_t length, int64_t batch,
                           void* sig, int64_t sig_stride, const void* seed, int64_t seed_stride,

@@ -363,8 +363,10 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         return fail(RPP_GB_OUT_OF_RESOURCES, "cudaEventCreate failed");
     int best = 0;
     float best_ms = 0.f;
-    for (int ci = 0; ci < ncand; ++ci) {
-        const int t = candidates[ci];
+    bool device_ok = true;
+    // one warm-up and two timed calls of candidate `t`; keeps the fastest
+    auto try_candidate = [&](int t) {
+        if (!device_ok) return;
         int rc = RPP_GB_SUCCESS;
         for (int rep = 0; rep < 3 && rc == RPP_GB_SUCCESS; ++rep) {
             if (rep == 1) cudaEventRecord(e0, s);
@@ -373,16 +375,33 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         }
         if (rc != RPP_GB_SUCCESS) {
             cudaGetLastError();  // configuration errors are not sticky; skip this candidate
-            continue;
+            return;
         }
         cudaEventRecord(e1, s);
-        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            device_ok = false;
+            return;
+        }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         if (best == 0 || ms < best_ms) {
             best = t;
             best_ms = ms;
         }
+    };
+    for (int ci = 0; ci < ncand; ++ci) try_candidate(candidates[ci]);
+    // A two-launch winner: its forward and reverse launches may prefer
+    // different CTA sizes.  Try other reverse sizes, then other forward sizes
+    // with the best reverse size.
+    if (best & rpp_gb::kScheduleSplit) {
+        constexpr int sh = rpp_gb::kScheduleReverseShift;
+        const int fwd = best & 1023;
+        const int flags = best & ((1 << sh) - 1) & ~1023;
+        for (int t : sizes)
+            if (t != fwd) try_candidate(flags | fwd | (t << sh));
+        const int rev = (best >> sh) & 1023 ? (best >> sh) & 1023 : fwd;
+        for (int t : sizes)
+            if (t != fwd) try_candidate(flags | t | (rev << sh));
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -156,9 +156,11 @@ struct PathBatch {
 // forward launch plus a reverse launch from the final signatures;
 // kScheduleForwardTopGlobal (with kScheduleSplit): the forward launch keeps
 // the top level in the output row in global memory (less shared memory per
-// CTA, more CTAs per SM).
+// CTA, more CTAs per SM); with kScheduleSplit, bits 16-25 (when not 0) give
+// the reverse launch its own CTA size (bits 0-9 then size the forward launch).
 constexpr int kScheduleSplit = 1 << 14;
 constexpr int kScheduleForwardTopGlobal = 1 << 15;
+constexpr int kScheduleReverseShift = 16;
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,

@@ -162,23 +162,30 @@ __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigSha
     const uint32_t W = Wd.value();
     T* S = sh.S;
     const T s0 = S[0];
+    // Each stage's chains (and then the levels of the last stage) form one
+    // run of coefficients: a thread that passes the end of one chain carries
+    // its offset into the next, so the small chains and levels are spread
+    // over the warps instead of all starting at warp 0.
     for (int j = 1; j < nmax; ++j) {
         const uint32_t wj = G.pw[j];
         const T* Sj = S + G.db[j];
+        uint32_t u = threadIdx.x;
         for (int n = j + 1; n <= nmax; ++n) {
             T* dst = chain(sg, sh.Tf, n, j);
             const T* prev = chain(sg, sh.Tf, n, j - 1);
             const T* xm = xc + (n - j + 1) * W;
-            for (uint32_t u = threadIdx.x; u < wj; u += blockDim.x) {
+            for (; u < wj; u += blockDim.x) {
                 uint32_t q, a;
                 Wd.divmod(u, q, a);
                 const T p = j == 1 ? s0 : prev[q];
                 dst[u] = fma(p, xm[a], Sj[u]);
             }
+            u -= wj;
         }
         __syncthreads();
     }
     const T* x1 = xc + W;
+    uint32_t v = threadIdx.x;
     for (int n = 1; n <= nmax; ++n) {
         const uint32_t wn = G.pw[n];
         T* Sn = n == G.depth ? sh.top : S + G.db[n];
@@ -207,12 +214,13 @@ __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigSha
             }
             continue;
         }
-        for (uint32_t u = threadIdx.x; u < wn; u += blockDim.x) {
+        for (; v < wn; v += blockDim.x) {
             uint32_t q, a;
-            Wd.divmod(u, q, a);
+            Wd.divmod(v, q, a);
             const T p = n == 1 ? s0 : prev[q];
-            Sn[u] = fma(p, x1[a], Sn[u]);
+            Sn[v] = fma(p, x1[a], Sn[v]);
         }
+        v -= wn;
     }
     set_increment(sg, sh, xc_next, x_next);
     __syncthreads();
@@ -243,8 +251,10 @@ __device__ __forceinline__ uint32_t partial_groups(uint32_t W) { return W > 16 ?
 
 // Finish a reverse step: grad_k from the partials (the stage-1 terms
 // sum_n Gh^n_1[a] S_0 folded in) and, when `update_g`, G_{k-1} from the
-// cotangent chains.  Runs between barriers; thread a < W reads G_1[a] before it
-// updates that same element (level-1 element u is updated by thread u).
+// cotangent chains.  Runs between barriers, beside the first recovery stage,
+// which runs on warp 0: the W gradient lanes are the first W threads of the
+// CTA's last warp(s), and each of them updates G_1[a] after reading it.  The
+// other levels of G form one run of coefficients over all threads.
 template <typename T>
 __device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const SigShared<T>& sh, T* grad_k,
                                                     bool update_g, uint32_t groups) {
@@ -252,8 +262,9 @@ __device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const
     const int D = G.depth;
     const uint32_t W = static_cast<uint32_t>(G.width);
     const T s0 = sh.S[0];
-    if (threadIdx.x < W) {
-        const uint32_t a = threadIdx.x;
+    const uint32_t gl = blockDim.x - ((W + 31u) & ~31u);  // (blockDim.x >= W, both multiples of 32 after rounding)
+    if (threadIdx.x >= gl && threadIdx.x < gl + W) {
+        const uint32_t a = threadIdx.x - gl;
         T v = T(0);
         for (int n = 1; n <= D; ++n) {
             const T* g1 = n == 1 ? (D == 1 ? sh.top : sh.G + G.db[1]) : chain(sg, sh.Tb, n, 1);
@@ -261,16 +272,24 @@ __device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const
         }
         for (uint32_t s = 0; s < groups; ++s) v += sh.part[s * W + a];
         grad_k[a] = v;
+        if (update_g && D > 1) {
+            T* G1 = sh.G + G.db[1];
+            T g = G1[a];
+            for (int n = 2; n <= D; ++n) g = fma(sh.num[n], chain(sg, sh.Tb, n, 1)[a], g);
+            G1[a] = g;
+        }
     }
     if (update_g) {
-        for (int i = 1; i < D; ++i) {
+        uint32_t u = threadIdx.x;
+        for (int i = 2; i < D; ++i) {
             const uint32_t wi = G.pw[i];
             T* Gi = sh.G + G.db[i];
-            for (uint32_t u = threadIdx.x; u < wi; u += blockDim.x) {
+            for (; u < wi; u += blockDim.x) {
                 T s = Gi[u];
                 for (int n = i + 1; n <= D; ++n) s = fma(sh.num[n - i + 1], chain(sg, sh.Tb, n, i)[u], s);
                 Gi[u] = s;
             }
+            u -= wi;
         }
     }
 }
@@ -697,7 +716,12 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
     // hold less shared memory per CTA (more CTAs per SM) than the fused one.
     const bool split = forward && sig && seed && grad && threads > 0 && (threads & kScheduleSplit);
     const bool fwd_top_global = split && (threads & kScheduleForwardTopGlobal);
-    if (split) threads &= ~(kScheduleSplit | kScheduleForwardTopGlobal);
+    int rev_threads = threads;
+    if (split) {
+        const int rev = (threads >> kScheduleReverseShift) & 1023;
+        threads &= (1 << 14) - 1;  // CTA size and cap
+        rev_threads = rev > 0 ? (threads & ~1023) | rev : threads;
+    }
     int mode = 0;
     if (forward) {
         mode |= kForward;
@@ -730,7 +754,7 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
         if (err == cudaSuccess && paths.counter) err = cudaMemsetAsync(paths.counter, 0, sizeof(unsigned int), s);
         if (err == cudaSuccess)
             err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad,
-                                      kBackward | kLoadFinal | kTopGlobal, threads);
+                                      kBackward | kLoadFinal | kTopGlobal, rev_threads);
     } else {
         err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
     }

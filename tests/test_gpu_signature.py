@@ -204,9 +204,13 @@ def test_autotuner_records_schedule_and_keeps_parity(orc):
     err, threads, ms = pkg.signature_tune(st, None, dev(incr), basis, B, length=L, out=sig, seed=dev(ell), grad=grad)
     assert err, err.message
     # schedule: threads per CTA in bits 0-9, CTA-per-SM cap in bits 10-13,
-    # bit 14 for the two-launch form
-    assert (threads & 1023) in (128, 192, 256, 320, 384, 512) and ((threads >> 10) & 15) in (0, 2, 3)
-    assert threads < (1 << 16) and ms > 0
+    # bit 14 for the two-launch form (bit 15: its forward top level in global
+    # memory; bits 16-25: its reverse launch's own CTA size)
+    sizes = (128, 192, 256, 320, 384, 512)
+    assert (threads & 1023) in sizes and ((threads >> 10) & 15) in (0, 2, 3)
+    assert (threads >> 26) == 0 and ((threads >> 16) & 1023) in (0,) + sizes
+    assert (threads >> 16) == 0 or threads & (1 << 14)
+    assert ms > 0
     esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
     assert_close(host(sig), esig, TOL_F64, "tuned signature")
     assert_close(host(grad), egrad, TOL_F64, "tuned gradient")
@@ -215,7 +219,8 @@ def test_autotuner_records_schedule_and_keeps_parity(orc):
 
 
 @pytest.mark.parametrize("schedule", [128, 256, 128 | (3 << 10), 192 | (2 << 10), 128 | (1 << 14),
-                                      256 | (1 << 14), 128 | (3 << 14), 320 | (3 << 14)])
+                                      256 | (1 << 14), 128 | (3 << 14), 320 | (3 << 14),
+                                      128 | (1 << 14) | (256 << 16), 256 | (3 << 14) | (128 << 16)])
 @pytest.mark.parametrize("ragged", [False, True])
 def test_every_schedule_matches_oracle(orc, schedule, ragged):
     """Each schedule the autotuner can pick (CTA size, a cap on CTAs per SM,
