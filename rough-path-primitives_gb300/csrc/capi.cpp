@@ -891,6 +891,35 @@ int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_d
     }
     std::vector<float> rval32(rval.begin(), rval.end());
 
+    // Sliced ELL copy (CsrDevice): rows by decreasing length, 32 per slice,
+    // entry-major within a slice.
+    std::vector<int32_t> rord(static_cast<size_t>(rows)), rlen(static_cast<size_t>(rows));
+    for (int64_t r = 0; r < rows; ++r) rord[r] = static_cast<int32_t>(r);
+    std::stable_sort(rord.begin(), rord.end(), [&](int32_t a, int32_t b) {
+        return roff[a + 1] - roff[a] > roff[b + 1] - roff[b];
+    });
+    const int64_t nslices = (rows + 31) / 32;
+    std::vector<int32_t> soff(static_cast<size_t>(nslices) + 1, 0);
+    int64_t ell_total = 0;
+    for (int64_t i = 0; i < rows; ++i) rlen[i] = roff[rord[i] + 1] - roff[rord[i]];
+    for (int64_t s = 0; s < nslices; ++s) {
+        ell_total += 32 * static_cast<int64_t>(rlen[static_cast<size_t>(32 * s)]);  // its longest row
+        if (ell_total > std::numeric_limits<int32_t>::max())
+            return fail(RPP_GB_OUT_OF_BOUNDS, "matrix too large for 32-bit sliced indices");
+        soff[s + 1] = static_cast<int32_t>(ell_total);
+    }
+    std::vector<int32_t> ecol(static_cast<size_t>(ell_total), 0);
+    std::vector<double> ev64(static_cast<size_t>(ell_total), 0.0);
+    for (int64_t i = 0; i < rows; ++i) {
+        const int64_t base = soff[static_cast<size_t>(i / 32)] + i % 32;
+        const int32_t r = rord[i];
+        for (int32_t k = 0; k < rlen[i]; ++k) {
+            ecol[base + 32 * k] = rcol[roff[r] + k];
+            ev64[base + 32 * k] = rval[roff[r] + k];
+        }
+    }
+    std::vector<float> ev32(ev64.begin(), ev64.end());
+
     int count = 0;
     cudaError_t err = cudaGetDeviceCount(&count);
     if (err != cudaSuccess) return cuda_status(err, "cudaGetDeviceCount");
@@ -904,8 +933,14 @@ int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_d
     const size_t b_v64 = align(std::max<size_t>(1, rval.size()) * sizeof(double));
     const size_t b_v32 = align(std::max<size_t>(1, rval32.size()) * sizeof(float));
     const size_t b_fault = 256;  // the fault word of the SpMM's bounded waits
+    const size_t b_ord = align(std::max<size_t>(1, rord.size()) * sizeof(int32_t));
+    const size_t b_soff = align(soff.size() * sizeof(int32_t));
+    const size_t b_ecol = align(std::max<size_t>(1, ecol.size()) * sizeof(int32_t));
+    const size_t b_ev64 = align(std::max<size_t>(1, ev64.size()) * sizeof(double));
+    const size_t b_ev32 = align(std::max<size_t>(1, ev32.size()) * sizeof(float));
+    const size_t b_csr = b_off + b_col + b_v64 + b_v32 + b_fault;
     char* block = nullptr;
-    if ((err = cudaMalloc(&block, b_off + b_col + b_v64 + b_v32 + b_fault)) != cudaSuccess)
+    if ((err = cudaMalloc(&block, b_csr + 2 * b_ord + b_soff + b_ecol + b_ev64 + b_ev32)) != cudaSuccess)
         return cuda_status(err, "cudaMalloc");
     auto* m = new (std::nothrow) rpp_gb_matrix;
     if (!m) {
@@ -919,6 +954,13 @@ int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_d
     auto* d_v64 = reinterpret_cast<double*>(block + b_off + b_col);
     auto* d_v32 = reinterpret_cast<float*>(block + b_off + b_col + b_v64);
     auto* d_fault = reinterpret_cast<uint32_t*>(block + b_off + b_col + b_v64 + b_v32);
+    char* sell = block + b_csr;
+    auto* d_ord = reinterpret_cast<int32_t*>(sell);
+    auto* d_len = reinterpret_cast<int32_t*>(sell + b_ord);
+    auto* d_soff = reinterpret_cast<int32_t*>(sell + 2 * b_ord);
+    auto* d_ecol = reinterpret_cast<int32_t*>(sell + 2 * b_ord + b_soff);
+    auto* d_ev64 = reinterpret_cast<double*>(sell + 2 * b_ord + b_soff + b_ecol);
+    auto* d_ev32 = reinterpret_cast<float*>(sell + 2 * b_ord + b_soff + b_ecol + b_ev64);
     if ((err = cudaMemset(d_fault, 0, sizeof(uint32_t))) != cudaSuccess) {
         cudaFree(block);
         delete m;
@@ -928,12 +970,22 @@ int rpp_gb_matrix_create(rpp_gb_matrix** matrix, int32_t format, int64_t outer_d
     if (err == cudaSuccess && nnz > 0) err = cudaMemcpy(d_col, rcol.data(), rcol.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
     if (err == cudaSuccess && nnz > 0) err = cudaMemcpy(d_v64, rval.data(), rval.size() * sizeof(double), cudaMemcpyHostToDevice);
     if (err == cudaSuccess && nnz > 0) err = cudaMemcpy(d_v32, rval32.data(), rval32.size() * sizeof(float), cudaMemcpyHostToDevice);
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        if (err == cudaSuccess && bytes > 0) err = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    up(d_ord, rord.data(), rord.size() * sizeof(int32_t));
+    up(d_len, rlen.data(), rlen.size() * sizeof(int32_t));
+    up(d_soff, soff.data(), soff.size() * sizeof(int32_t));
+    up(d_ecol, ecol.data(), ecol.size() * sizeof(int32_t));
+    up(d_ev64, ev64.data(), ev64.size() * sizeof(double));
+    up(d_ev32, ev32.data(), ev32.size() * sizeof(float));
     if (err != cudaSuccess) {
         cudaFree(block);
         delete m;
         return cuda_status(err, "cudaMemcpy");
     }
-    m->csr = rpp_gb::CsrDevice{d_off, d_col, d_v64, d_v32, rows, cols, nnz, format == RPP_GB_CSC, d_fault};
+    m->csr = rpp_gb::CsrDevice{d_off,  d_col, d_v64,  d_v32, rows,   cols,   nnz,  format == RPP_GB_CSC,
+                               d_fault, d_ord, d_len, d_soff, d_ecol, d_ev64, d_ev32};
     *matrix = m;
     return ok();
 }

@@ -26,38 +26,12 @@
 #include "ft_device.cuh"
 #include "launch_util.cuh"
 #include "ops.hpp"
+#include "sell.cuh"
 
 namespace rpp_gb {
 namespace {
 
 using namespace ftdev;
-
-template <typename T>
-__device__ __forceinline__ const T* csr_vals(const CsrDevice& m);
-template <>
-__device__ __forceinline__ const double* csr_vals<double>(const CsrDevice& m) {
-    return m.values64;
-}
-template <>
-__device__ __forceinline__ const float* csr_vals<float>(const CsrDevice& m) {
-    return m.values32;
-}
-
-// y[r] = alpha * sum_e val[e] x[col[e]] for r < rows; zeros up to `zero_to`
-// when the matrix came from CSC (its product zeroes the whole output view).
-template <typename T>
-__device__ __forceinline__ void csr_rows(const CsrDevice& m, const T* __restrict__ x, T* y, int64_t zero_to, T alpha) {
-    const T* vals = csr_vals<T>(m);
-    const int64_t end = m.zero_rest ? zero_to : m.rows;
-    for (int64_t r = threadIdx.x; r < end; r += blockDim.x) {
-        T acc = T(0);
-        if (r < m.rows) {
-            const int32_t e0 = __ldg(m.offsets + r), e1 = __ldg(m.offsets + r + 1);
-            for (int32_t e = e0; e < e1; ++e) acc = fma(__ldg(vals + e), x[__ldg(m.cols + e)], acc);
-        }
-        y[r] = alpha * acc;
-    }
-}
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_log_to_lie(Geometry G, CsrDevice m, TArg<T> x, int lo, int hi, T* out,
@@ -76,7 +50,7 @@ __global__ void __launch_bounds__(256) k_log_to_lie(Geometry G, CsrDevice m, TAr
         if (!st.commit(G.fault)) return;
         intermediate_one(G, IntermediateKind::Log, s_log, lo, hi, X, none);
         __syncthreads();
-        csr_rows(m, s_log + G.db[lo], out + b * out_stride, out_size, alpha);
+        sell_rows(m, s_log + G.db[lo], out + b * out_stride, out_size, alpha);
         bulk_stage_reuse();
     }
 }
@@ -103,7 +77,7 @@ __global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const 
         if (fm) M = {mult.at(b), mult.lo, imin(mult.hi, G.depth)};
         for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) s_x[i] = T(0);
         if (!st.commit(G.fault)) return;
-        csr_rows(m, l, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
+        sell_rows(m, l, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
         __syncthreads();
         const Opnd<T> X{s_x, imax(1, lo), hi};
         intermediate_one(G, fm ? IntermediateKind::FMExp : IntermediateKind::Exp, s_o, out.lo, ohi, X, M);

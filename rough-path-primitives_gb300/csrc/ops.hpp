@@ -66,6 +66,19 @@ struct CsrDevice {
     int64_t nnz;
     bool zero_rest;  // matrix came from CSC: zero the whole out view first
     uint32_t* fault; // fault word for expired bounded waits (see Geometry::fault)
+    // Sliced copy for the SpMM kernels (sliced ELL, 32 rows per slice): the
+    // rows in decreasing number of entries (ties in row order) are cut into
+    // slices of 32, and entry k of the slice's row l sits at
+    // slice_off[s] + 32*k + l.  A warp takes a slice and lane l walks its row:
+    // the warp's loads of entry k are one contiguous span, and the rows of a
+    // warp have nearly equal lengths, so its FMA instructions run with nearly
+    // all lanes active (a warp issues as many as its longest row has entries).
+    const int32_t* order;      // rows: the row at sorted position i
+    const int32_t* row_len;    // rows: its number of entries
+    const int32_t* slice_off;  // slices + 1 (multiples of 32)
+    const int32_t* ell_cols;   // slice_off[slices]; padding is never read
+    const double* ell_v64;
+    const float* ell_v32;
 };
 
 template <typename T>

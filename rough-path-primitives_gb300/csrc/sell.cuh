@@ -1,0 +1,50 @@
+// sell.cuh -- one sparse matrix times one vector by a whole CTA, over the
+// sliced copy of the matrix (CsrDevice: 32 rows per slice, rows by decreasing
+// length, entry-major within a slice).  Used by the batched SpMM (sparse.cu)
+// and by the fused Lie <-> tensor kernels (lie_fused.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ops.hpp"
+
+namespace rpp_gb {
+
+template <typename T>
+__device__ __forceinline__ const T* sell_values(const CsrDevice& m);
+template <>
+__device__ __forceinline__ const double* sell_values<double>(const CsrDevice& m) {
+    return m.ell_v64;
+}
+template <>
+__device__ __forceinline__ const float* sell_values<float>(const CsrDevice& m) {
+    return m.ell_v32;
+}
+
+// y[r] = alpha * sum_k val(r, k) x[col(r, k)] for every row r, entries in the
+// row's CSR order (so the sum is rounded exactly as a row-by-row CSR product
+// would round it); with a matrix that came from CSC, y[i] = alpha * 0 for
+// rows <= i < zero_to as well (its product zeroes the whole output view).
+// Warp w of the CTA takes slices w, w + warps, ...; blockDim.x is a multiple
+// of 32.  Each y[r] is written once, by one thread.
+template <typename T>
+__device__ __forceinline__ void sell_rows(const CsrDevice& m, const T* __restrict__ x, T* y, int64_t zero_to,
+                                          T alpha) {
+    const T* vals = sell_values<T>(m);
+    const uint32_t lane = threadIdx.x & 31u;
+    const int64_t slices = (m.rows + 31) / 32;
+    for (int64_t s = threadIdx.x >> 5; s < slices; s += blockDim.x >> 5) {
+        const int64_t i = s * 32 + lane;
+        if (i >= m.rows) continue;
+        const int32_t r = __ldg(m.order + i), len = __ldg(m.row_len + i);
+        const int32_t base = __ldg(m.slice_off + s) + static_cast<int32_t>(lane);
+        T acc = T(0);
+        for (int32_t k = 0; k < len; ++k) acc = fma(__ldg(vals + base + 32 * k), x[__ldg(m.ell_cols + base + 32 * k)], acc);
+        y[r] = alpha * acc;
+    }
+    if (m.zero_rest)
+        for (int64_t i = m.rows + threadIdx.x; i < zero_to; i += blockDim.x) y[i] = alpha * T(0);
+}
+
+}  // namespace rpp_gb

@@ -4,28 +4,19 @@
 // The reference launches one CTA per vector and, for CSC, one thread per
 // non-zero with a binary search for its column and a block-scope atomic add
 // into global memory (include/rpp/gpu/block/operations/linalg/
-// sparse_matrix_vector.hpp:150-185).  Here the matrix is CSR (CSC inputs are
-// transposed once when the handle is created), each CTA stages one argument
-// vector in shared memory and each thread owns output rows: no atomics, a
-// deterministic summation order, coalesced writes.
+// sparse_matrix_vector.hpp:150-185).  Here the matrix is converted once, when
+// the handle is created, to CSR (CSC inputs transposed) and to a sliced copy
+// of 32 rows per slice (sell.cuh); each CTA stages one argument vector in
+// shared memory and each thread owns output rows: no atomics and a
+// deterministic summation order.
 #include "bulk_stage.cuh"
 #include "common.cuh"
 #include "launch_util.cuh"
 #include "ops.hpp"
+#include "sell.cuh"
 
 namespace rpp_gb {
 namespace {
-
-template <typename T>
-__device__ __forceinline__ const T* csr_values(const CsrDevice& m);
-template <>
-__device__ __forceinline__ const double* csr_values<double>(const CsrDevice& m) {
-    return m.values64;
-}
-template <>
-__device__ __forceinline__ const float* csr_values<float>(const CsrDevice& m) {
-    return m.values32;
-}
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_stride, int64_t out_size,
@@ -36,9 +27,6 @@ __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_s
     T* s_arg = reinterpret_cast<T*>(smem_raw + kBulkHeader);
     uint32_t phase = 0;
     if (staged) bulk_stage_init(bar);
-    const T* vals = csr_values<T>(m);
-    const int64_t rows = m.rows;
-    const int64_t write_end = m.zero_rest ? out_size : rows;
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         const T* x = arg + b * arg_stride;
         T* y = out + b * out_stride;
@@ -47,14 +35,7 @@ __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_s
             x = st.add_span(s_arg, x, 0, static_cast<uint32_t>(arg_size));
             if (!st.commit(m.fault)) return;
         }
-        for (int64_t r = threadIdx.x; r < write_end; r += blockDim.x) {
-            T acc = T(0);
-            if (r < rows) {
-                const int32_t e0 = __ldg(m.offsets + r), e1 = __ldg(m.offsets + r + 1);
-                for (int32_t e = e0; e < e1; ++e) acc = fma(__ldg(vals + e), x[__ldg(m.cols + e)], acc);
-            }
-            y[r] = alpha * acc;
-        }
+        sell_rows(m, x, y, out_size, alpha);
         if (staged) bulk_stage_reuse();
     }
 }
