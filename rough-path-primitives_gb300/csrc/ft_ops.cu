@@ -120,23 +120,25 @@ __global__ void __launch_bounds__(256) k_intermediate(Geometry G, IntermediateKi
     }
 }
 
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    return v;
-}
-
 // Adjoint multiplies (include/rpp/operations/basic/ft_adj_lmul.hpp,
 // ft_adj_rmul.hpp; semantics as tests/rpp/ft_adjoint_test_helper.hpp:55-87):
 //   left:  out[m][j] = sum_p sum_u op[p][u] arg[m+p][u*W^m + j]
 //   right: out[m][j] = sum_p sum_v op[p][v] arg[m+p][j*W^p + v]
-// Output degrees with fewer coefficients than warps give each coefficient a
-// group of nwarps / W^m warps (the low degrees hold the longest sums: at W16 D3
-// the degree-0 coefficient alone has 4 369 terms); each warp of the group sums
-// every (group*32)-th term and the group's partials are added in warp order
-// after a barrier.  Other narrow degrees (fewer coefficients than threads)
-// give each coefficient a warp; wide degrees give each coefficient a thread.
+// The terms (p, u) of one coefficient form one run (a thread's offset is
+// carried from split degree to split degree, so short splits do not leave
+// lanes idle).  Output degrees with at least one coefficient per thread give
+// each coefficient a thread.  Narrower degrees give each coefficient a group
+// of g threads that stride over its terms and are then summed in a fixed
+// order:
+//  * right: g (a power of two) consecutive threads per coefficient, so their
+//    reads arg[m+p][j*W^p + u] are consecutive; summed by an xor-shuffle
+//    tree inside the warp, then (g > 32) the group's warps in warp order;
+//  * left: threads t = j + r*W^m, so consecutive threads read consecutive
+//    arg[m+p][u*W^m + j] (one thread per u would put the lanes of a warp
+//    W^m elements apart, in few banks); lanes of a warp with the same j are
+//    summed by a shuffle tree, then the warps' partials in warp order.
+// The degree-0 coefficient of W16 D3 alone has 4 369 terms; W2 D12 has
+// about 8 000 terms per output degree, most of them in the narrow degrees.
 template <typename T>
 __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> out, TArg<T> op,
                                                  TArg<T> arg, int64_t batch, int staged) {
@@ -144,11 +146,12 @@ __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> o
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     T* sm = reinterpret_cast<T*>(smem_raw + kBulkHeader);
     const uint32_t pd = staged_elems<T>(G.dim);
+    T* s_part = sm + (staged ? 2 * pd : 0);  // one partial per thread
     uint32_t phase = 0;
     if (staged) bulk_stage_init(bar);
     const int D = G.depth;
     const int ohi = imin(out.hi, D), phi = imin(op.hi, D), ahi = imin(arg.hi, D);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const uint32_t nt = blockDim.x, t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         const T* P = op.at(b);
         const T* A = arg.at(b);
@@ -162,58 +165,68 @@ __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> o
         for (int m = out.lo; m <= ohi; ++m) {
             const uint32_t wm = G.pw[m];
             const int pmin = imax(op.lo, arg.lo - m), pmax = imin(phi, ahi - m);
-            if (wm < static_cast<uint32_t>(nwarps)) {
-                T* s_part = sm + (staged ? 2 * pd : 0);
-                const uint32_t group = static_cast<uint32_t>(nwarps) / wm;
-                const uint32_t j = static_cast<uint32_t>(warp) / group;
-                const uint32_t rank = static_cast<uint32_t>(warp) - j * group;
+            // terms u = first, first + stride, ... of coefficient j, over the
+            // split degrees in turn
+            auto terms = [&](uint32_t j, uint32_t first, uint32_t stride) {
                 T acc = T(0);
-                if (j < wm) {
-                    const uint32_t step = group * 32;
-                    for (int p = pmin; p <= pmax; ++p) {
-                        const uint32_t wp = G.pw[p];
-                        const T* Pp = P + G.db[p];
-                        const T* Ap = A + G.db[m + p];
-                        for (uint32_t u = rank * 32 + lane; u < wp; u += step)
-                            acc = fma(Pp[u], left ? Ap[u * wm + j] : Ap[j * wp + u], acc);
-                    }
+                uint32_t u = first;
+                for (int p = pmin; p <= pmax; ++p) {
+                    const uint32_t wp = G.pw[p];
+                    const T* Pp = P + G.db[p];
+                    const T* Ap = A + G.db[m + p];
+                    if (left)
+                        for (; u < wp; u += stride) acc = fma(Pp[u], Ap[u * wm + j], acc);
+                    else
+                        for (; u < wp; u += stride) acc = fma(Pp[u], Ap[j * wp + u], acc);
+                    u -= wp;
                 }
-                acc = warp_sum(acc);
-                if (lane == 0) s_part[warp] = acc;
-                __syncthreads();
-                if (j < wm && rank == 0 && lane == 0) {
-                    T v = s_part[warp];
-                    for (uint32_t r = 1; r < group; ++r) v += s_part[warp + r];
-                    o[G.db[m] + j] = v;
-                }
-                __syncthreads();
-            } else if (wm < blockDim.x) {
-                for (uint32_t j = warp; j < wm; j += nwarps) {
-                    T acc = T(0);
-                    for (int p = pmin; p <= pmax; ++p) {
-                        const uint32_t wp = G.pw[p];
-                        const T* Pp = P + G.db[p];
-                        const T* Ap = A + G.db[m + p];
-                        for (uint32_t u = lane; u < wp; u += 32)
-                            acc = fma(Pp[u], left ? Ap[u * wm + j] : Ap[j * wp + u], acc);
+                return acc;
+            };
+            if (wm >= nt) {
+                for (uint32_t j = t; j < wm; j += nt) o[G.db[m] + j] = terms(j, 0, 1);
+            } else if (!left) {
+                uint32_t g = 1;
+                while (2 * g * wm <= nt) g *= 2;
+                const uint32_t j = t / g, r = t % g;
+                T acc = j < wm ? terms(j, r, g) : T(0);
+                for (uint32_t off = (g < 32 ? g : 32) / 2; off > 0; off /= 2) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+                if (g <= 32) {
+                    if (j < wm && r == 0) o[G.db[m] + j] = acc;
+                } else {
+                    if (lane == 0) s_part[warp] = acc;
+                    __syncthreads();
+                    const uint32_t gw = g / 32;
+                    if (j < wm && r == 0) {
+                        T v = s_part[warp];
+                        for (uint32_t k = 1; k < gw; ++k) v += s_part[warp + k];
+                        o[G.db[m] + j] = v;
                     }
-                    acc = warp_sum(acc);
-                    if (lane == 0) o[G.db[m] + j] = acc;
+                    __syncthreads();
                 }
             } else {
-                for (uint32_t j = threadIdx.x; j < wm; j += blockDim.x) {
-                    T acc = T(0);
-                    for (int p = pmin; p <= pmax; ++p) {
-                        const uint32_t wp = G.pw[p];
-                        const T* Pp = P + G.db[p];
-                        const T* Ap = A + G.db[m + p];
-                        if (left)
-                            for (uint32_t u = 0; u < wp; ++u) acc = fma(Pp[u], Ap[u * wm + j], acc);
-                        else
-                            for (uint32_t u = 0; u < wp; ++u) acc = fma(Pp[u], Ap[j * wp + u], acc);
+                const uint32_t g = nt / wm;
+                const uint32_t j = t % wm, r = t / wm;
+                T acc = r < g ? terms(j, r, g) : T(0);
+                if (wm < 32) {
+                    // lanes l, l + wm, l + 2wm, ... of a warp share j
+                    for (uint32_t off = wm; off < 32u; off *= 2u) {
+                        const T x = __shfl_down_sync(0xffffffffu, acc, off);
+                        if (lane + off < 32u) acc += x;
                     }
-                    o[G.db[m] + j] = acc;
+                    if (lane < wm) s_part[warp * wm + t % wm] = acc;
+                } else {
+                    s_part[t] = acc;
                 }
+                __syncthreads();
+                if (t < wm) {
+                    T v = T(0);
+                    if (wm < 32)
+                        for (uint32_t w = 0; w < (nt >> 5); ++w) v += s_part[w * wm + t];
+                    else
+                        for (uint32_t k = 0; k < g; ++k) v += s_part[t + k * wm];
+                    o[G.db[m] + t] = v;
+                }
+                __syncthreads();
             }
         }
         bulk_stage_reuse();
@@ -406,7 +419,7 @@ cudaError_t launch_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
     const size_t smem_need = 2 * static_cast<size_t>(staged_elems<T>(g.dim)) * sizeof(T);
-    const size_t part = kBulkHeader + 32 * sizeof(T);  // the mbarrier and one partial per warp
+    const size_t part = kBulkHeader + 256 * sizeof(T);  // the mbarrier and one partial per thread
     const int staged = smem_need + part <= kStageLimit && smem_need + part <= static_cast<size_t>(dev.max_smem_optin);
     const size_t smem = (staged ? smem_need : 0) + part;
     const int threads = threads_for(g.pw[g.depth]);
