@@ -90,6 +90,42 @@ __device__ void product_levels(const Geometry& G, T* dst, int lo, int hi, const 
 // (up to D! times the result) stay far from FP32 overflow.
 constexpr int kScaledHornerMaxDepth = 12;
 
+// 1/d and d as T (0 < d <= kMaxDepth + 1) and 1/d! (d <= kScaledHornerMaxDepth),
+// each rounded once at compile time: the values a run-time division gives (it
+// is correctly rounded; d! is exact in both types up to 12!), without the
+// FP64 instruction sequence a division costs every thread of the CTA on every
+// Horner round.
+template <typename T>
+struct Reciprocals {
+    T inv[kMaxDepth + 2];
+    T num[kMaxDepth + 2];
+    T inv_fact[kScaledHornerMaxDepth + 1];
+    constexpr Reciprocals() : inv{}, num{}, inv_fact{} {
+        for (int d = 1; d < kMaxDepth + 2; ++d) {
+            inv[d] = T(1) / T(d);
+            num[d] = T(d);
+        }
+        T f = T(1);
+        inv_fact[0] = T(1);
+        for (int d = 1; d <= kScaledHornerMaxDepth; ++d) {
+            f *= T(d);
+            inv_fact[d] = T(1) / f;
+        }
+    }
+};
+static __constant__ Reciprocals<double> kRecip64{};
+static __constant__ Reciprocals<float> kRecip32{};
+template <typename T>
+__device__ __forceinline__ const Reciprocals<T>& recip();
+template <>
+__device__ __forceinline__ const Reciprocals<double>& recip<double>() {
+    return kRecip64;
+}
+template <>
+__device__ __forceinline__ const Reciprocals<float>& recip<float>() {
+    return kRecip32;
+}
+
 template <typename T>
 __device__ void intermediate_one(const Geometry& G, IntermediateKind kind, T* o, int olo, int ohi,
                                  Opnd<T> X, Opnd<T> M) {
@@ -115,8 +151,8 @@ __device__ void intermediate_one(const Geometry& G, IntermediateKind kind, T* o,
     for (int d = D; d > 0; --d) {
         const int tmax = D - d + 1;
         const Opnd<T> Xt{X.p, imax(1, X.lo), imin(X.hi, tmax)};
-        const T inv = T(1) / static_cast<T>(d);
-        c *= static_cast<T>(d);
+        const T inv = recip<T>().inv[d];
+        c *= recip<T>().num[d];
         if (kind == IntermediateKind::Exp) {
             if (scaled) product_levels<T, false>(G, o, olo, ohi, none, T(0), Opnd<T>{o, olo, ohi}, Xt, T(1), true);
             else product_levels(G, o, olo, ohi, none, T(0), Opnd<T>{o, olo, ohi}, Xt, inv, true);
@@ -126,15 +162,14 @@ __device__ void intermediate_one(const Geometry& G, IntermediateKind kind, T* o,
             if (scaled) product_levels<T, false>(G, o, olo, ohi, M, c, Opnd<T>{o, olo, ohi}, Xt, T(1), true);
             else product_levels(G, o, olo, ohi, M, T(1), Opnd<T>{o, olo, ohi}, Xt, inv, true);
         } else {
-            const T val = ((d % 2 == 0) ? T(-1) : T(1)) / static_cast<T>(d);
-            if (threadIdx.x == 0 && olo == 0) o[0] += val;
+            if (threadIdx.x == 0 && olo == 0) o[0] += (d % 2 == 0) ? -inv : inv;  // (-1)^{d+1} / d
             __syncthreads();
             const int thi = imin(ohi, tmax);
             product_levels<T, false>(G, o, olo, thi, none, T(0), Opnd<T>{o, olo, thi}, Xt, T(1), true);
         }
     }
     if (scaled && olo <= ohi) {  // o = p_1 / D!
-        const T s = T(1) / c;
+        const T s = recip<T>().inv_fact[D];  // 1 / c, c = D! exactly
         for (uint32_t i = G.db[olo] + threadIdx.x; i < G.db[ohi + 1]; i += blockDim.x) o[i] *= s;
         __syncthreads();
     }

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(256) k_exp_letter_vjp(Geometry G, const T* H, 
         if (threadIdx.x == 0) E[0] = T(1);
         __syncthreads();
         for (int n = 1; n <= D; ++n) {
-            const T inv = T(1) / static_cast<T>(n);
+            const T inv = recip<T>().inv[n];
             for (uint32_t i = threadIdx.x; i < G.pw[n]; i += blockDim.x) {
                 uint32_t q, a;
                 G.divw.divmod(i, q, a);
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(256) k_exp_letter_vjp(Geometry G, const T* H, 
         }
         T acc = T(0);
         for (int n = D; n >= 1; --n) {
-            const T inv = T(1) / static_cast<T>(n);
+            const T inv = recip<T>().inv[n];
             const uint32_t wp = G.pw[n - 1];
             const T* En1 = E + G.db[n - 1];
             const T* Ebn = Eb + G.db[n];
