@@ -26,17 +26,22 @@ __device__ __forceinline__ const float* sell_values<float>(const CsrDevice& m) {
 // row's CSR order (so the sum is rounded exactly as a row-by-row CSR product
 // would round it); with a matrix that came from CSC, y[i] = alpha * 0 for
 // rows <= i < zero_to as well (its product zeroes the whole output view).
-// Warp w of the CTA takes slices w, w + warps, ...; blockDim.x is a multiple
-// of 32.  Each y[r] is written once, by one thread.
+// Slices go to warps in zig-zag order (round k: warp w takes slice
+// k*warps + w for even k, k*warps + warps-1-w for odd k): slices are sorted
+// longest first, so plain round-robin would give warp 0 the longest slice of
+// every round (at W5 D5 the t2l matrix's busiest warp then has 1.65 times the
+// mean work, 1.43 times in zig-zag order).  blockDim.x is a multiple of 32.
+// Each y[r] is written once, by one thread.
 template <typename T>
 __device__ __forceinline__ void sell_rows(const CsrDevice& m, const T* __restrict__ x, T* y, int64_t zero_to,
                                           T alpha) {
     const T* vals = sell_values<T>(m);
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int64_t slices = (m.rows + 31) / 32;
-    for (int64_t s = threadIdx.x >> 5; s < slices; s += blockDim.x >> 5) {
+    for (int64_t round = 0; round * nw < slices; ++round) {
+        const int64_t s = round * nw + ((round & 1) ? nw - 1 - w : w);
         const int64_t i = s * 32 + lane;
-        if (i >= m.rows) continue;
+        if (s >= slices || i >= m.rows) continue;
         const int32_t r = __ldg(m.order + i), len = __ldg(m.row_len + i);
         const int32_t base = __ldg(m.slice_off + s) + static_cast<int32_t>(lane);
         T acc = T(0);
