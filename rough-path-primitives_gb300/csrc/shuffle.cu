@@ -278,6 +278,45 @@ struct AdjItems {
     }
 };
 
+// Where letter a's blocks of op degree m and merged degree N start: the op
+// coefficient of word u is OP[ob0 + a*obs + u], the argument coefficient of
+// merged word s is ARG[ab0 + a*abs + s].
+struct AdjBlocks {
+    uint32_t ob0, obs, ab0, abs;
+    __device__ AdjBlocks(const Geometry& G, int kind, int m, int N) {
+        if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
+            ob0 = G.db[m + 1];
+            obs = G.pw[m];
+            ab0 = G.db[N + 1];
+            abs = G.pw[N];
+        } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
+            ob0 = G.db[m];
+            obs = 0;
+            ab0 = G.db[N + 1];
+            abs = G.pw[N];
+        } else {
+            ob0 = G.db[m];
+            obs = 0;
+            ab0 = G.db[N];
+            abs = 0;
+        }
+    }
+};
+
+// The W^k FMAs of one item for letter a (k = min(m, 2); m >= 1): op words
+// uh*W^2 + u1*W + u0 (m >= 2) or u0 (m = 1), argument at `ar` + u0*c0 + u1*c1.
+template <typename T>
+__device__ __forceinline__ T item_terms(const T* __restrict__ op, const T* __restrict__ ar, uint32_t W, int m,
+                                        uint32_t c0, uint32_t c1, T acc) {
+    if (m >= 2) {
+        for (uint32_t u1 = 0; u1 < W; ++u1, op += W, ar += c1)
+            for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
+    } else {
+        for (uint32_t u0 = 0; u0 < W; ++u0) acc = fma(op[u0], ar[u0 * c0], acc);
+    }
+    return acc;
+}
+
 template <typename T>
 __device__ T adjoint_coeff(const Geometry& G, int kind, int n, uint32_t j, const T* __restrict__ OP, int olo,
                            int ohi, const T* __restrict__ ARG, int alo, int ahi, uint32_t first, uint32_t step) {
@@ -457,6 +496,82 @@ __device__ T adjoint_coeff_seq(const Geometry& G, int kind, int n, uint32_t j, c
     return acc;
 }
 
+// The left adjoint's sum for one thread alone: plain nested loops over
+// (m, M, u_hi), with the prefix letters innermost -- the walk that places w's and u_hi's
+// letters is the same for every letter a, so a thread pays it once per
+// (letters x W^k) FMAs.  (The warp cursor keeps the letter in the item key:
+// items W times larger would leave the lanes of a low-degree coefficient's
+// warp unbalanced -- measured 39 % slower on left_hs_adj_lmul at W5 D5.)
+template <typename T>
+__device__ T adjoint_coeff_seq_left(const Geometry& G, int kind, int n, uint32_t j, const T* __restrict__ OP, int olo,
+                               int ohi, const T* __restrict__ ARG, int alo, int ahi) {
+    const uint32_t W = static_cast<uint32_t>(G.width);
+    int nw = n, mlo, mhi;
+    uint32_t w = j, a0 = 0, a1 = 1;
+    if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
+        a1 = W;
+        mlo = imax(0, imax(olo - 1, alo - 1 - n));
+        mhi = imin(ohi - 1, ahi - 1 - n);
+    } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
+        if (n == 0) return T(0);
+        const uint32_t tail = G.pw[n - 1];
+        const uint32_t a = j / tail;
+        nw = n - 1;
+        w = j - a * tail;
+        a0 = a;
+        a1 = a + 1;
+        mlo = imax(olo, alo - n);
+        mhi = imin(ohi, ahi - n);
+    } else {
+        mlo = imax(olo, alo - n);
+        mhi = imin(ohi, ahi - n);
+    }
+    T acc = T(0);
+    for (int m = mhi; m >= mlo; --m) {
+        const int N = nw + m;
+        const AdjBlocks bl(G, kind, m, N);
+        if (m == 0) {
+            for (uint32_t a = a0; a < a1; ++a) acc = fma(OP[bl.ob0 + a * bl.obs], ARG[bl.ab0 + a * bl.abs + w], acc);
+            continue;
+        }
+        const uint32_t nhi = m <= 1 ? 1u : G.pw[m - 2];
+        uint32_t M = (1u << m) - 1u;
+        const uint32_t last = M << nw;
+        for (;;) {
+            const uint32_t b0 = M & (0u - M);
+            const uint32_t r0 = M ^ b0;
+            const uint32_t b1 = m >= 2 ? r0 & (0u - r0) : 0u;
+            const uint32_t rest = r0 ^ b1;
+            const uint32_t c0 = G.pw[__ffs(b0) - 1];
+            const uint32_t c1 = m >= 2 ? G.pw[__ffs(b1) - 1] : 0u;
+            for (uint32_t uh = 0; uh < nhi; ++uh) {
+                uint32_t wq = w, uq = uh, base = 0, p = 1;
+                for (int bpos = 0; bpos < N; ++bpos) {
+                    const uint32_t bit = 1u << bpos;
+                    if (!((b0 | b1) & bit)) {
+                        const bool from_u = (rest & bit) != 0;
+                        const uint32_t src = from_u ? uq : wq;
+                        uint32_t q, r;
+                        G.divw.divmod(src, q, r);
+                        if (from_u) uq = q;
+                        else wq = q;
+                        base += r * p;
+                    }
+                    p *= W;
+                }
+                const uint32_t ou = m >= 2 ? uh * W * W : 0u;
+                for (uint32_t a = a0; a < a1; ++a)
+                    acc = item_terms(OP + bl.ob0 + a * bl.obs + ou, ARG + bl.ab0 + a * bl.abs + base, W, m, c0, c1,
+                                     acc);
+            }
+            if (M == last) break;
+            const uint32_t ripple = M + b0;
+            M = ripple | (((ripple ^ M) >> 2) >> (__ffs(M) - 1));
+        }
+    }
+    return acc;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind, TArg<T> out, TArg<T> op,
                                                         TArg<T> arg, int64_t batch, T beta, int staged,
@@ -504,7 +619,9 @@ __global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind
                     int n;
                     uint32_t j;
                     locate(ord, k, n, j);
-                    const T acc = adjoint_coeff_seq<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi);
+                    const T acc = kind == static_cast<int>(ShuffleAdjKind::HalfL)
+                                      ? adjoint_coeff_seq_left<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi)
+                                      : adjoint_coeff_seq<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi);
                     o[G.db[n] + j] = beta == T(1) ? acc : beta * acc;
                 }
             }
