@@ -17,6 +17,7 @@
 // splits are walked with one divide-by-W per step (FastDiv), no per-element
 // degree search.
 #include <cstdio>
+#include <type_traits>
 
 #include "bulk_stage.cuh"
 #include "common.cuh"
@@ -29,7 +30,9 @@ namespace {
 
 using namespace ftdev;
 
-template <typename T>
+// Scale = false: beta is 1 and the products are not multiplied by it (one
+// FP64 multiply per output coefficient saved; chosen by the launcher).
+template <typename T, bool Scale>
 __global__ void __launch_bounds__(256) k_product(Geometry G, ProductKind kind, TArg<T> out,
                                                  TArg<T> x, TArg<T> y, TArg<T> z, int64_t batch,
                                                  T alpha, T beta, int staged) {
@@ -78,10 +81,10 @@ __global__ void __launch_bounds__(256) k_product(Geometry G, ProductKind kind, T
             L.p = st.add(sm + pd, L.p, L.lo, imin(L.hi, G.depth), G);
             R.p = st.add(sm + 2 * pd, R.p, R.lo, imin(R.hi, G.depth), G);
             if (!st.commit(G.fault)) return;
-            product_levels(G, dst, out.lo, imin(out.hi, G.depth), add, alpha, L, R, beta, false);
+            product_levels<T, Scale>(G, dst, out.lo, imin(out.hi, G.depth), add, alpha, L, R, beta, false);
             bulk_stage_reuse();
         } else {
-            product_levels(G, dst, out.lo, imin(out.hi, G.depth), add, alpha, L, R, beta, true);
+            product_levels<T, Scale>(G, dst, out.lo, imin(out.hi, G.depth), add, alpha, L, R, beta, true);
         }
     }
 }
@@ -378,18 +381,21 @@ cudaError_t launch_product(const Geometry& g, const DeviceInfo& dev, cudaStream_
                            TArg<T> out, TArg<T> x, TArg<T> y, TArg<T> z, int64_t batch, double alpha,
                            double beta) {
     if (batch <= 0) return cudaSuccess;
-    constexpr auto kernel = k_product<T>;
-    cudaError_t err = allow_large_smem<kernel>(dev);
-    if (err != cudaSuccess) return err;
     const size_t smem_need = kBulkHeader + 3 * static_cast<size_t>(staged_elems<T>(g.dim)) * sizeof(T);
     const int staged = smem_need <= kStageLimit && smem_need <= static_cast<size_t>(dev.max_smem_optin);
     const size_t smem = staged ? smem_need : 0;
     const int threads = threads_for(g.pw[g.depth]);
-    dim3 grid;
-    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
-    kernel<<<grid, threads, smem, s>>>(g, kind, out, x, y, z, batch, static_cast<T>(alpha),
-                                       static_cast<T>(beta), staged);
-    return cudaGetLastError();
+    auto run = [&](auto kernel) {
+        cudaError_t err = allow_large_smem<decltype(kernel)::value>(dev);
+        if (err != cudaSuccess) return err;
+        dim3 grid;
+        if ((err = batch_grid(decltype(kernel)::value, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+        decltype(kernel)::value<<<grid, threads, smem, s>>>(g, kind, out, x, y, z, batch, static_cast<T>(alpha),
+                                                            static_cast<T>(beta), staged);
+        return cudaGetLastError();
+    };
+    if (static_cast<T>(beta) == T(1)) return run(std::integral_constant<decltype(&k_product<T, false>), &k_product<T, false>>{});
+    return run(std::integral_constant<decltype(&k_product<T, true>), &k_product<T, true>>{});
 }
 
 template <typename T>

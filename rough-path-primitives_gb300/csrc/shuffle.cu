@@ -278,31 +278,6 @@ struct AdjItems {
     }
 };
 
-// Where letter a's blocks of op degree m and merged degree N start: the op
-// coefficient of word u is OP[ob0 + a*obs + u], the argument coefficient of
-// merged word s is ARG[ab0 + a*abs + s].
-struct AdjBlocks {
-    uint32_t ob0, obs, ab0, abs;
-    __device__ AdjBlocks(const Geometry& G, int kind, int m, int N) {
-        if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
-            ob0 = G.db[m + 1];
-            obs = G.pw[m];
-            ab0 = G.db[N + 1];
-            abs = G.pw[N];
-        } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
-            ob0 = G.db[m];
-            obs = 0;
-            ab0 = G.db[N + 1];
-            abs = G.pw[N];
-        } else {
-            ob0 = G.db[m];
-            obs = 0;
-            ab0 = G.db[N];
-            abs = 0;
-        }
-    }
-};
-
 // The W^k FMAs of one item for letter a (k = min(m, 2); m >= 1): op words
 // uh*W^2 + u1*W + u0 (m >= 2) or u0 (m = 1), argument at `ar` + u0*c0 + u1*c1.
 template <typename T>
@@ -497,46 +472,30 @@ __device__ T adjoint_coeff_seq(const Geometry& G, int kind, int n, uint32_t j, c
 }
 
 // The left adjoint's sum for one thread alone: plain nested loops over
-// (m, M, u_hi), with the prefix letters innermost -- the walk that places w's and u_hi's
-// letters is the same for every letter a, so a thread pays it once per
-// (letters x W^k) FMAs.  (The warp cursor keeps the letter in the item key:
-// items W times larger would leave the lanes of a low-degree coefficient's
-// warp unbalanced -- measured 39 % slower on left_hs_adj_lmul at W5 D5.)
+// (m, M, u_hi), with the prefix letters innermost -- the walk that places w's
+// and u_hi's letters is the same for every letter a, so a thread pays it once
+// per W x W^k FMAs.  (The warp cursor keeps the letter in the item key: items
+// W times larger would leave the lanes of a low-degree coefficient's warp
+// unbalanced -- measured 39 % slower on left_hs_adj_lmul at W5 D5.)  Letter
+// a's op block of degree m + 1 starts at db[m+1] + a W^m, its argument block
+// of degree n + m + 1 at db[n+m+1] + a W^{n+m}.
 template <typename T>
-__device__ T adjoint_coeff_seq_left(const Geometry& G, int kind, int n, uint32_t j, const T* __restrict__ OP, int olo,
-                               int ohi, const T* __restrict__ ARG, int alo, int ahi) {
+__device__ T adjoint_coeff_seq_left(const Geometry& G, int n, uint32_t w, const T* __restrict__ OP, int olo,
+                                    int ohi, const T* __restrict__ ARG, int alo, int ahi) {
     const uint32_t W = static_cast<uint32_t>(G.width);
-    int nw = n, mlo, mhi;
-    uint32_t w = j, a0 = 0, a1 = 1;
-    if (kind == static_cast<int>(ShuffleAdjKind::HalfL)) {
-        a1 = W;
-        mlo = imax(0, imax(olo - 1, alo - 1 - n));
-        mhi = imin(ohi - 1, ahi - 1 - n);
-    } else if (kind == static_cast<int>(ShuffleAdjKind::HalfR)) {
-        if (n == 0) return T(0);
-        const uint32_t tail = G.pw[n - 1];
-        const uint32_t a = j / tail;
-        nw = n - 1;
-        w = j - a * tail;
-        a0 = a;
-        a1 = a + 1;
-        mlo = imax(olo, alo - n);
-        mhi = imin(ohi, ahi - n);
-    } else {
-        mlo = imax(olo, alo - n);
-        mhi = imin(ohi, ahi - n);
-    }
+    const int mlo = imax(0, imax(olo - 1, alo - 1 - n));
+    const int mhi = imin(ohi - 1, ahi - 1 - n);
     T acc = T(0);
     for (int m = mhi; m >= mlo; --m) {
-        const int N = nw + m;
-        const AdjBlocks bl(G, kind, m, N);
+        const int N = n + m;
+        const uint32_t ob0 = G.db[m + 1], obs = G.pw[m], ab0 = G.db[N + 1], abs = G.pw[N];
         if (m == 0) {
-            for (uint32_t a = a0; a < a1; ++a) acc = fma(OP[bl.ob0 + a * bl.obs], ARG[bl.ab0 + a * bl.abs + w], acc);
+            for (uint32_t a = 0; a < W; ++a) acc = fma(OP[ob0 + a * obs], ARG[ab0 + a * abs + w], acc);
             continue;
         }
         const uint32_t nhi = m <= 1 ? 1u : G.pw[m - 2];
         uint32_t M = (1u << m) - 1u;
-        const uint32_t last = M << nw;
+        const uint32_t last = M << n;
         for (;;) {
             const uint32_t b0 = M & (0u - M);
             const uint32_t r0 = M ^ b0;
@@ -560,9 +519,8 @@ __device__ T adjoint_coeff_seq_left(const Geometry& G, int kind, int n, uint32_t
                     p *= W;
                 }
                 const uint32_t ou = m >= 2 ? uh * W * W : 0u;
-                for (uint32_t a = a0; a < a1; ++a)
-                    acc = item_terms(OP + bl.ob0 + a * bl.obs + ou, ARG + bl.ab0 + a * bl.abs + base, W, m, c0, c1,
-                                     acc);
+                for (uint32_t a = 0; a < W; ++a)
+                    acc = item_terms(OP + ob0 + a * obs + ou, ARG + ab0 + a * abs + base, W, m, c0, c1, acc);
             }
             if (M == last) break;
             const uint32_t ripple = M + b0;
@@ -620,7 +578,7 @@ __global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind
                     uint32_t j;
                     locate(ord, k, n, j);
                     const T acc = kind == static_cast<int>(ShuffleAdjKind::HalfL)
-                                      ? adjoint_coeff_seq_left<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi)
+                                      ? adjoint_coeff_seq_left<T>(G, n, j, P, op.lo, ohi, A, arg.lo, ahi)
                                       : adjoint_coeff_seq<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi);
                     o[G.db[n] + j] = beta == T(1) ? acc : beta * acc;
                 }
