@@ -21,6 +21,7 @@
 // do not fit.
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <type_traits>
 
 #include "bulk_stage.cuh"
 #include "ft_device.cuh"
@@ -33,7 +34,7 @@ namespace {
 
 using namespace ftdev;
 
-template <typename T>
+template <typename T, bool Scale>
 __global__ void __launch_bounds__(256) k_log_to_lie(Geometry G, CsrDevice m, TArg<T> x, int lo, int hi, T* out,
                                                    int64_t out_stride, int64_t out_size, int64_t batch, T alpha) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -50,12 +51,12 @@ __global__ void __launch_bounds__(256) k_log_to_lie(Geometry G, CsrDevice m, TAr
         if (!st.commit(G.fault)) return;
         intermediate_one(G, IntermediateKind::Log, s_log, lo, hi, X, none);
         __syncthreads();
-        sell_rows(m, s_log + G.db[lo], out + b * out_stride, out_size, alpha);
+        sell_rows<Scale>(m, s_log + G.db[lo], out + b * out_stride, out_size, alpha);
         bulk_stage_reuse();
     }
 }
 
-template <typename T>
+template <typename T, bool Scale>
 __global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const T* lie, int64_t lie_stride, int lo,
                                                 int hi, TArg<T> out, TArg<T> mult, int64_t batch, T alpha) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const 
         if (fm) M = {mult.at(b), mult.lo, imin(mult.hi, G.depth)};
         for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) s_x[i] = T(0);
         if (!st.commit(G.fault)) return;
-        sell_rows(m, l, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
+        sell_rows<Scale>(m, l, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
         __syncthreads();
         const Opnd<T> X{s_x, imax(1, lo), hi};
         intermediate_one(G, fm ? IntermediateKind::FMExp : IntermediateKind::Exp, s_o, out.lo, ohi, X, M);
@@ -107,16 +108,21 @@ cudaError_t launch_log_to_lie(const Geometry& g, const DeviceInfo& dev, cudaStre
                               TArg<T> x, int lo, int hi, T* out, int64_t out_stride, int64_t out_size, int64_t batch,
                               double alpha) {
     if (batch <= 0) return cudaSuccess;
-    constexpr auto kernel = k_log_to_lie<T>;
-    cudaError_t err = allow_large_smem<kernel>(dev);
-    if (err != cudaSuccess) return err;
     const size_t smem = log_to_lie_smem(g, sizeof(T));
     if (smem > static_cast<size_t>(dev.max_smem_optin)) return cudaErrorInvalidConfiguration;
     const int threads = threads_for(g.pw[g.depth]);
-    dim3 grid;
-    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
-    kernel<<<grid, threads, smem, s>>>(g, m, x, lo, hi, out, out_stride, out_size, batch, static_cast<T>(alpha));
-    return cudaGetLastError();
+    auto run = [&](auto kernel) {
+        constexpr auto k = decltype(kernel)::value;
+        cudaError_t err = allow_large_smem<k>(dev);
+        if (err != cudaSuccess) return err;
+        dim3 grid;
+        if ((err = batch_grid(k, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+        k<<<grid, threads, smem, s>>>(g, m, x, lo, hi, out, out_stride, out_size, batch, static_cast<T>(alpha));
+        return cudaGetLastError();
+    };
+    if (static_cast<T>(alpha) == T(1))
+        return run(std::integral_constant<decltype(&k_log_to_lie<T, false>), &k_log_to_lie<T, false>>{});
+    return run(std::integral_constant<decltype(&k_log_to_lie<T, true>), &k_log_to_lie<T, true>>{});
 }
 
 template <typename T>
@@ -124,17 +130,22 @@ cudaError_t launch_lie_exp(const Geometry& g, const DeviceInfo& dev, cudaStream_
                            const T* lie, int64_t lie_stride, int lo, int hi, TArg<T> out, TArg<T> mult,
                            int64_t batch, double alpha) {
     if (batch <= 0) return cudaSuccess;
-    constexpr auto kernel = k_lie_exp<T>;
-    cudaError_t err = allow_large_smem<kernel>(dev);
-    if (err != cudaSuccess) return err;
     const size_t smem = lie_exp_smem(g, sizeof(T), mult.p != nullptr);
     if (smem > static_cast<size_t>(dev.max_smem_optin) || m.cols_dim > static_cast<int64_t>(g.dim))
         return cudaErrorInvalidConfiguration;
     const int threads = threads_for(g.pw[g.depth]);
-    dim3 grid;
-    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
-    kernel<<<grid, threads, smem, s>>>(g, m, lie, lie_stride, lo, hi, out, mult, batch, static_cast<T>(alpha));
-    return cudaGetLastError();
+    auto run = [&](auto kernel) {
+        constexpr auto k = decltype(kernel)::value;
+        cudaError_t err = allow_large_smem<k>(dev);
+        if (err != cudaSuccess) return err;
+        dim3 grid;
+        if ((err = batch_grid(k, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+        k<<<grid, threads, smem, s>>>(g, m, lie, lie_stride, lo, hi, out, mult, batch, static_cast<T>(alpha));
+        return cudaGetLastError();
+    };
+    if (static_cast<T>(alpha) == T(1))
+        return run(std::integral_constant<decltype(&k_lie_exp<T, false>), &k_lie_exp<T, false>>{});
+    return run(std::integral_constant<decltype(&k_lie_exp<T, true>), &k_lie_exp<T, true>>{});
 }
 
 #define RPP_GB_INSTANTIATE_LIE_FUSED(T)                                                                           \

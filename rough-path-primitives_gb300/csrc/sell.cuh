@@ -31,8 +31,9 @@ __device__ __forceinline__ const float* sell_values<float>(const CsrDevice& m) {
 // longest first, so plain round-robin would give warp 0 the longest slice of
 // every round (at W5 D5 the t2l matrix's busiest warp then has 1.65 times the
 // mean work, 1.43 times in zig-zag order).  blockDim.x is a multiple of 32.
-// Each y[r] is written once, by one thread.
-template <typename T>
+// Each y[r] is written once, by one thread.  Scale = false: alpha is 1 and
+// is not multiplied in (chosen by the launchers at compile time).
+template <bool Scale, typename T>
 __device__ __forceinline__ void sell_rows(const CsrDevice& m, const T* __restrict__ x, T* y, int64_t zero_to,
                                           T alpha) {
     const T* vals = sell_values<T>(m);
@@ -46,10 +47,10 @@ __device__ __forceinline__ void sell_rows(const CsrDevice& m, const T* __restric
         const int32_t base = __ldg(m.slice_off + s) + static_cast<int32_t>(lane);
         T acc = T(0);
         for (int32_t k = 0; k < len; ++k) acc = fma(__ldg(vals + base + 32 * k), x[__ldg(m.ell_cols + base + 32 * k)], acc);
-        y[r] = alpha * acc;
+        y[r] = Scale ? alpha * acc : acc;
     }
     if (m.zero_rest)
-        for (int64_t i = m.rows + threadIdx.x; i < zero_to; i += blockDim.x) y[i] = alpha * T(0);
+        for (int64_t i = m.rows + threadIdx.x; i < zero_to; i += blockDim.x) y[i] = Scale ? alpha * T(0) : T(0);
 }
 
 }  // namespace rpp_gb

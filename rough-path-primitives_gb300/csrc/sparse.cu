@@ -9,6 +9,8 @@
 // of 32 rows per slice (sell.cuh); each CTA stages one argument vector in
 // shared memory and each thread owns output rows: no atomics and a
 // deterministic summation order.
+#include <type_traits>
+
 #include "bulk_stage.cuh"
 #include "common.cuh"
 #include "launch_util.cuh"
@@ -18,7 +20,7 @@
 namespace rpp_gb {
 namespace {
 
-template <typename T>
+template <typename T, bool Scale>
 __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_stride, int64_t out_size,
                                               const T* arg, int64_t arg_stride, int64_t arg_size,
                                               int64_t batch, T alpha, int staged) {
@@ -35,7 +37,7 @@ __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_s
             x = st.add_span(s_arg, x, 0, static_cast<uint32_t>(arg_size));
             if (!st.commit(m.fault)) return;
         }
-        sell_rows(m, x, y, out_size, alpha);
+        sell_rows<Scale>(m, x, y, out_size, alpha);
         if (staged) bulk_stage_reuse();
     }
 }
@@ -47,18 +49,22 @@ cudaError_t launch_spmm(const CsrDevice& m, const DeviceInfo& dev, cudaStream_t 
                         int64_t out_stride, int64_t out_size, const T* arg, int64_t arg_stride,
                         int64_t arg_size, int64_t batch, double alpha) {
     if (batch <= 0) return cudaSuccess;
-    constexpr auto kernel = k_spmm<T>;
-    cudaError_t err = allow_large_smem<kernel>(dev);
-    if (err != cudaSuccess) return err;
     const size_t need = kBulkHeader + static_cast<size_t>(staged_elems<T>(static_cast<uint32_t>(arg_size))) * sizeof(T);
     const int staged = arg_size < (int64_t{1} << 31) && need <= 96 * 1024;
     const size_t smem = staged ? need : 0;
     const int threads = 256;
-    dim3 grid;
-    if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
-    kernel<<<grid, threads, smem, s>>>(m, out, out_stride, out_size, arg, arg_stride, arg_size, batch,
-                                       static_cast<T>(alpha), staged);
-    return cudaGetLastError();
+    auto run = [&](auto kernel) {
+        constexpr auto k = decltype(kernel)::value;
+        cudaError_t err = allow_large_smem<k>(dev);
+        if (err != cudaSuccess) return err;
+        dim3 grid;
+        if ((err = batch_grid(k, dev, threads, smem, batch, grid)) != cudaSuccess) return err;
+        k<<<grid, threads, smem, s>>>(m, out, out_stride, out_size, arg, arg_stride, arg_size, batch,
+                                      static_cast<T>(alpha), staged);
+        return cudaGetLastError();
+    };
+    if (static_cast<T>(alpha) == T(1)) return run(std::integral_constant<decltype(&k_spmm<T, false>), &k_spmm<T, false>>{});
+    return run(std::integral_constant<decltype(&k_spmm<T, true>), &k_spmm<T, true>>{});
 }
 
 template cudaError_t launch_spmm<float>(const CsrDevice&, const DeviceInfo&, cudaStream_t, float*, int64_t,
