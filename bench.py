@@ -649,20 +649,18 @@ def main():
         elapsed = float(t.item())
     value = world * batch * args.steps / elapsed
 
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: rpp_gb_signature_host
+    # copies each step's increments and seeds in from pinned host memory and the
+    # signatures and gradients back out, in two chunks whose copies overlap the
+    # other chunk's kernels (the schedule recorded by the tuner above)
     incr_p = torch.from_numpy(incr_h).pin_memory()
     ell_p = torch.from_numpy(ell_h).pin_memory()
     sig_p = torch.empty(batch, dim, dtype=torch.float64).pin_memory()
     grad_p = torch.empty(incr_h.shape, dtype=torch.float64).pin_memory()
-    incr_d, ell_d = torch.empty_like(incr), torch.empty_like(ell)
 
     def e2e_step():
-        incr_d.copy_(incr_p, non_blocking=True)
-        ell_d.copy_(ell_p, non_blocking=True)
-        pkg.signature(strat, cfg, incr_d, basis, batch, length=LENGTH, out=sig, seed=ell_d,
-                      grad=grad, schedule=pinned).raise_if_failed()
-        sig_p.copy_(sig, non_blocking=True)
-        grad_p.copy_(grad, non_blocking=True)
+        pkg.signature_host(strat, cfg, incr_p, basis, batch, length=LENGTH, out=sig_p, seed=ell_p,
+                           grad=grad_p).raise_if_failed()
 
     for _ in range(2):
         e2e_step()

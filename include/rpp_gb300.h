@@ -364,6 +364,25 @@ int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int
                               int64_t batch, const void* sig, int64_t sig_stride,
                               const void* seed, int64_t seed_stride, void* grad);
 
+/* rpp_gb_signature over HOST buffers (no counterpart in the reference), for
+ * callers whose paths live in host memory: incr, sig, seed and grad are host
+ * pointers (same layouts and strides as rpp_gb_signature; equal-length paths
+ * only, length > 0).  The batch is processed in chunks of `chunk` paths (0:
+ * two chunks) that alternate between two internal streams; on each, a chunk
+ * is copied in, computed with the schedule recorded for this shape and copied
+ * out, so one chunk's copies overlap another chunk's kernels.  Pinned host
+ * memory lets the copies run asynchronously (pageable memory works but
+ * serialises them).  Stream-ordered: the internal streams start after the work
+ * already on `stream`, and `stream` waits for them, so the host outputs are
+ * complete once `stream` has passed the call (e.g. after
+ * cudaStreamSynchronize).  Device buffers for two chunks are allocated
+ * stream-ordered and released at the end.  The results equal
+ * rpp_gb_signature's on device copies of the same arrays. */
+int rpp_gb_signature_host(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
+                          const void* incr, int64_t length, int64_t batch, void* sig,
+                          int64_t sig_stride, const void* seed, int64_t seed_stride,
+                          void* grad, int64_t chunk);
+
 /* rpp_gb_signature without any device allocation (no counterpart in the
  * reference).  For callers that cannot allocate device memory at call time:
  * runtimes that own all device memory through their own allocator and forbid

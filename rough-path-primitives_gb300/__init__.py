@@ -664,6 +664,30 @@ def signature(strategy, config, increments, basis, num_batches, *, length=None, 
     return _status(lib.rpp_gb_signature(*args))
 
 
+def signature_host(strategy, config, increments, basis, num_batches, *, length, out=None, out_stride=None,
+                   seed=None, seed_stride=None, grad=None, chunk=0) -> Error:
+    """Signatures of equal-length paths from HOST tensors (rpp_gb_signature_host):
+    ``increments`` [num_batches * length, width], ``out``, ``seed`` and ``grad``
+    are CPU tensors (pinned, for the copies to overlap the kernels) with the
+    layouts of ``signature``.  The batch runs in chunks of ``chunk`` paths
+    (0: two) on two internal streams; ``out`` and ``grad`` are complete once
+    the configuration's stream has been synchronised."""
+    dt = strategy.torch_dtype()
+    for t in (increments, out, seed, grad):
+        if t is None:
+            continue
+        if getattr(t, "is_cuda", True):
+            raise ValueError("signature_host takes host (CPU) tensors")
+        if t.dtype != dt or not t.is_contiguous():
+            raise ValueError(f"host tensors must be contiguous {dt}")
+    dim = basis.size()
+    lib = _lib.load()
+    return _status(lib.rpp_gb_signature_host(
+        basis.plan(strategy.device), _cfg(config).handle(strategy.device), strategy.dtype_code(),
+        _ptr(increments), int(length), num_batches, _ptr(out), dim if out_stride is None else out_stride,
+        _ptr(seed), dim if seed_stride is None else seed_stride, _ptr(grad), int(chunk)))
+
+
 def exp_letter_vjp(strategy, config, cotangent, x, dx, basis, num_batches, *, cotangent_stride=None,
                    x_stride=None, dx_stride=None, x_offset=0, dx_offset=0) -> Error:
     """dx_a = sum_w H[w] d exp(x)[w] / dx_a for degree-one x (rpp_gb_exp_letter_vjp):

@@ -87,6 +87,7 @@ SIGNATURES = {
     "rpp_gb_signature": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp],
     "rpp_gb_signature_backward": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp],
     "rpp_gb_signature_static_scratch": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp],
+    "rpp_gb_signature_host": [_vp, _vp, _i32, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64],
     "rpp_gb_fma_peak": [_i32, _i32, _DBLP],
     "rpp_gb_signature_tune": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp,
                               ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)],

@@ -417,6 +417,92 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
                             true, best);
 }
 
+// Host buffers in, host buffers out: chunks of the batch go round two
+// internal streams, each chunk copied in, computed (the recorded schedule of
+// this shape, as rpp_gb_signature) and copied out on its stream, so one
+// chunk's copies overlap another chunk's kernels.  Paths are independent, so
+// the results equal rpp_gb_signature's on device copies of the same arrays.
+cudaError_t copy_rows(void* dst, size_t dst_pitch, const void* src, size_t src_pitch, size_t row_bytes, size_t rows,
+                      cudaMemcpyKind kind, cudaStream_t s) {
+    if (rows == 0) return cudaSuccess;
+    if (dst_pitch == row_bytes && src_pitch == row_bytes)
+        return cudaMemcpyAsync(dst, src, row_bytes * rows, kind, s);
+    return cudaMemcpy2DAsync(dst, dst_pitch, src, src_pitch, row_bytes, rows, kind, s);
+}
+
+template <typename T>
+int run_signature_host(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const void* incr, int64_t length,
+                       int64_t batch, void* sig, int64_t sig_stride, const void* seed, int64_t seed_stride,
+                       void* grad, int64_t chunk) {
+    const auto& g = plan->geometry;
+    if (length <= 0) return fail(RPP_GB_INVALID_ARGUMENT, "host-buffer signatures need equal path lengths > 0");
+    if (!incr) return fail(RPP_GB_INVALID_ARGUMENT, "increments are NULL");
+    if ((seed == nullptr) != (grad == nullptr)) return fail(RPP_GB_INVALID_ARGUMENT, "seed and grad must be given together");
+    if (!sig && !grad) return fail(RPP_GB_INVALID_ARGUMENT, "nothing to compute");
+    const int64_t dim = g.dim, row = length * g.width;
+    if ((sig && sig_stride < dim) || (seed && seed_stride < dim))
+        return fail(RPP_GB_INVALID_ARGUMENT, "stride shorter than the tensor dimension");
+    if (chunk <= 0) chunk = (batch + 1) / 2;
+    chunk = std::min(chunk, batch);
+    const size_t ts = sizeof(T);
+    const size_t per_path = static_cast<size_t>(2 * row + (sig ? dim : 0) + (seed ? dim : 0));
+    const size_t bytes = per_path * static_cast<size_t>(chunk) * ts;
+
+    cudaStream_t st[2] = {nullptr, nullptr};
+    cudaEvent_t ready = nullptr, done[2] = {nullptr, nullptr};
+    char* buf[2] = {nullptr, nullptr};
+    cudaError_t err = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+    for (int i = 0; i < 2 && err == cudaSuccess; ++i) {
+        err = cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+    }
+    if (err == cudaSuccess) err = cudaEventRecord(ready, s);  // after the caller's earlier work
+    for (int i = 0; i < 2 && err == cudaSuccess; ++i) {
+        err = cudaStreamWaitEvent(st[i], ready, 0);
+        if (err == cudaSuccess) err = cudaMallocAsync(reinterpret_cast<void**>(&buf[i]), bytes, st[i]);
+    }
+    int rc = err == cudaSuccess ? static_cast<int>(RPP_GB_SUCCESS) : cuda_status(err, "host-buffer signature setup");
+    for (int64_t b0 = 0, c = 0; b0 < batch && rc == RPP_GB_SUCCESS; b0 += chunk, ++c) {
+        const int i = static_cast<int>(c & 1);
+        const int64_t nb = std::min(chunk, batch - b0);
+        T* d_incr = reinterpret_cast<T*>(buf[i]);
+        T* d_grad = grad ? d_incr + chunk * row : nullptr;
+        T* d_sig = sig ? d_incr + 2 * chunk * row : nullptr;
+        T* d_seed = seed ? d_incr + 2 * chunk * row + (sig ? chunk * dim : 0) : nullptr;
+        const auto* h_incr = static_cast<const char*>(incr) + b0 * row * ts;
+        err = cudaMemcpyAsync(d_incr, h_incr, static_cast<size_t>(nb * row) * ts, cudaMemcpyHostToDevice, st[i]);
+        if (err == cudaSuccess && seed)
+            err = copy_rows(d_seed, dim * ts, static_cast<const char*>(seed) + b0 * seed_stride * ts, seed_stride * ts,
+                            dim * ts, nb, cudaMemcpyHostToDevice, st[i]);
+        if (err != cudaSuccess) {
+            rc = cuda_status(err, "host-to-device copy");
+            break;
+        }
+        rc = run_signature<T>(plan, st[i], dtype, d_incr, nullptr, length, nb, d_sig, dim, d_seed, dim, d_grad, true);
+        if (rc != RPP_GB_SUCCESS) break;
+        if (sig)
+            err = copy_rows(static_cast<char*>(sig) + b0 * sig_stride * ts, sig_stride * ts, d_sig, dim * ts, dim * ts,
+                            nb, cudaMemcpyDeviceToHost, st[i]);
+        if (err == cudaSuccess && grad)
+            err = cudaMemcpyAsync(static_cast<char*>(grad) + b0 * row * ts, d_grad, static_cast<size_t>(nb * row) * ts,
+                                  cudaMemcpyDeviceToHost, st[i]);
+        if (err != cudaSuccess) rc = cuda_status(err, "device-to-host copy");
+    }
+    // release the buffers after their last use, then order the caller's
+    // stream after both internal streams
+    for (int i = 0; i < 2; ++i) {
+        if (!st[i]) continue;
+        if (buf[i]) cudaFreeAsync(buf[i], st[i]);
+        if (done[i] && cudaEventRecord(done[i], st[i]) == cudaSuccess) cudaStreamWaitEvent(s, done[i], 0);
+    }
+    for (int i = 0; i < 2; ++i) {
+        if (done[i]) cudaEventDestroy(done[i]);
+        if (st[i]) cudaStreamDestroy(st[i]);
+    }
+    if (ready) cudaEventDestroy(ready);
+    return rc;
+}
+
 }  // namespace
 
 // Shuffle algebra: operand conversion and order computation shared by the
@@ -1144,6 +1230,18 @@ int rpp_gb_signature_backward(const rpp_gb_plan* plan, rpp_gb_stream stream, int
                                            sig_stride, seed, seed_stride, grad, false)
                    : run_signature<float>(plan, s, dtype, incr, offsets, length, batch, const_cast<void*>(sig),
                                           sig_stride, seed, seed_stride, grad, false);
+    });
+}
+
+int rpp_gb_signature_host(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype, const void* incr,
+                          int64_t length, int64_t batch, void* sig, int64_t sig_stride, const void* seed,
+                          int64_t seed_stride, void* grad, int64_t chunk) {
+    return with_plan(plan, dtype, batch, [&] {
+        auto s = static_cast<cudaStream_t>(stream);
+        return dtype == RPP_GB_F64 ? run_signature_host<double>(plan, s, dtype, incr, length, batch, sig, sig_stride,
+                                                                seed, seed_stride, grad, chunk)
+                                   : run_signature_host<float>(plan, s, dtype, incr, length, batch, sig, sig_stride,
+                                                               seed, seed_stride, grad, chunk);
     });
 }
 

@@ -249,3 +249,59 @@ def test_every_schedule_matches_oracle(orc, schedule, ragged):
     assert_close(host(sig), esig, TOL_F64, f"signature, schedule {schedule}")
     assert_close(host(grad), egrad, TOL_F64, f"gradient, schedule {schedule}")
 
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("W,D,B,L,chunk", [(5, 5, 7, 16, 0), (5, 5, 7, 16, 3), (3, 4, 10, 9, 1), (4, 4, 5, 8, 64),
+                                           (2, 6, 9, 12, 4)])
+def test_host_buffers_equal_device_path(W, D, B, L, chunk, dtype):
+    """rpp_gb_signature_host: host tensors in and out, the batch in chunks on
+    two internal streams -- bit-identical to the device call (paths are
+    independent), with strided host outputs and every output combination."""
+    rng = np.random.default_rng(W * 100 + D * 10 + B + chunk)
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(dtype)
+    incr = torch.from_numpy(rng.normal(0, 1 / np.sqrt(L), (B * L, W))).to(dtype)
+    ell = torch.from_numpy(rng.uniform(-1, 1, (B, dim))).to(dtype)
+    want_sig = torch.empty(B, dim, dtype=dtype, device="cuda")
+    want_grad = torch.empty(B * L, W, dtype=dtype, device="cuda")
+    assert pkg.signature(st, None, incr.cuda(), basis, B, length=L, out=want_sig, seed=ell.cuda(), grad=want_grad)
+    torch.cuda.synchronize()
+    # strided host signatures (stride dim + 3), contiguous gradients
+    sig_h = torch.full((B, dim + 3), float("nan"), dtype=dtype).pin_memory()
+    grad_h = torch.full((B * L, W), float("nan"), dtype=dtype).pin_memory()
+    seed_h = torch.zeros(B, dim + 2, dtype=dtype)
+    seed_h[:, :dim] = ell
+    err = pkg.signature_host(st, None, incr.pin_memory(), basis, B, length=L, out=sig_h, out_stride=dim + 3,
+                             seed=seed_h.pin_memory(), seed_stride=dim + 2, grad=grad_h, chunk=chunk)
+    assert err, err.message
+    torch.cuda.synchronize()
+    assert torch.equal(sig_h[:, :dim], want_sig.cpu()), "signatures differ from the device path"
+    assert torch.isnan(sig_h[:, dim:]).all(), "wrote outside the signature rows"
+    assert torch.equal(grad_h, want_grad.cpu()), "gradients differ from the device path"
+    # signatures only, then gradients only, each against the device call that
+    # asks for the same outputs (a different output set is a different schedule
+    # key, and the gradient's reduction order follows the CTA size)
+    sig_only = torch.empty(B, dim, dtype=dtype).pin_memory()
+    assert pkg.signature_host(st, None, incr, basis, B, length=L, out=sig_only, chunk=chunk)
+    grad_only = torch.empty(B * L, W, dtype=dtype)
+    assert pkg.signature_host(st, None, incr, basis, B, length=L, seed=ell.contiguous(), grad=grad_only, chunk=chunk)
+    only_sig = torch.empty(B, dim, dtype=dtype, device="cuda")
+    assert pkg.signature(st, None, incr.cuda(), basis, B, length=L, out=only_sig)
+    only_grad = torch.empty(B * L, W, dtype=dtype, device="cuda")
+    assert pkg.signature(st, None, incr.cuda(), basis, B, length=L, seed=ell.cuda(), grad=only_grad)
+    torch.cuda.synchronize()
+    assert torch.equal(sig_only, only_sig.cpu())
+    assert torch.equal(grad_only, only_grad.cpu())
+
+
+def test_host_buffers_refusals():
+    basis = pkg.TensorBasis(3, 3)
+    st = pkg.GB300Strategy(torch.float64)
+    incr = torch.zeros(8, 3, dtype=torch.float64)
+    out = torch.zeros(2, basis.size(), dtype=torch.float64)
+    err = pkg.signature_host(st, None, incr, basis, 2, length=0, out=out)
+    assert not err and err.code == pkg.ErrorCode.InvalidArgument
+    with pytest.raises(ValueError):
+        pkg.signature_host(st, None, incr.cuda(), basis, 2, length=4, out=out)
