@@ -39,6 +39,7 @@
 // scaled increments | 1/m | one partial per thread | G levels 0..D-1 |
 // cotangent chains.
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
 #include "launch_util.cuh"
@@ -151,12 +152,25 @@ __device__ __forceinline__ void load_row(T (&r)[WT], const T* src) {
     for (int a = 0; a < WT; ++a) r[a] = src[a];
 }
 
+// FP32 forward step four coefficients at a time (W a multiple of 4, state in
+// shared memory).  In FP32 the element loop is bound by instruction issue and
+// shared-memory wavefronts, not by the FMA pipe: an index split, three loads
+// and a store per FMA.  Four consecutive coefficients of a level share their
+// prefix coefficient and take four consecutive increment letters, so one
+// thread does them with 16-byte loads and stores.  Alignment: level n >= 1
+// starts at db[n] = 1 (mod 4) for W = 0 (mod 4), so the state array is placed
+// with S + 1 on a 16-byte boundary; chain links of stages j >= 1 lie multiples
+// of W apart from Tf + choff[1], which is placed on a 16-byte boundary too, and
+// so are the scaled increments.
+template <typename T, int WT>
+constexpr bool kVec4 = std::is_same<T, float>::value && WT > 0 && WT % 4 == 0;
+
 // One forward step S <- S (x) exp(x).  `nmax` = D when the top level is
 // maintained, D-1 when it is not needed (gradient-only calls).  Ends with a
 // barrier, after which xc_next holds the next step's scaled increment.
 template <typename T, int WT>
 __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigShared<T>& sh, const T* xc,
-                                             T* xc_next, T x_next, int nmax, bool top_global) {
+                                             T* xc_next, T x_next, int nmax, bool top_global, bool vec4) {
     const Geometry& G = sg.g;
     const Width<WT> Wd(G);
     const uint32_t W = Wd.value();
@@ -169,6 +183,28 @@ __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigSha
     for (int j = 1; j < nmax; ++j) {
         const uint32_t wj = G.pw[j];
         const T* Sj = S + G.db[j];
+        if constexpr (kVec4<T, WT>) {
+            if (vec4) {
+                uint32_t v = threadIdx.x;  // groups of four coefficients
+                for (int n = j + 1; n <= nmax; ++n) {
+                    const T* prev = chain(sg, sh.Tf, n, j - 1);
+                    float4* dst = reinterpret_cast<float4*>(chain(sg, sh.Tf, n, j));
+                    const T* xm = xc + (n - j + 1) * WT;
+                    const uint32_t groups = wj / 4;
+                    for (; v < groups; v += blockDim.x) {
+                        const uint32_t u = 4 * v, q = u / WT, a = u % WT;
+                        const T pq = j == 1 ? s0 : prev[q];
+                        const float4 sv = reinterpret_cast<const float4*>(Sj)[v];
+                        const float4 xv = *reinterpret_cast<const float4*>(xm + a);
+                        dst[v] = make_float4(fmaf(pq, xv.x, sv.x), fmaf(pq, xv.y, sv.y), fmaf(pq, xv.z, sv.z),
+                                             fmaf(pq, xv.w, sv.w));
+                    }
+                    v -= groups;
+                }
+                __syncthreads();
+                continue;
+            }
+        }
         uint32_t u = threadIdx.x;
         for (int n = j + 1; n <= nmax; ++n) {
             T* dst = chain(sg, sh.Tf, n, j);
@@ -185,8 +221,32 @@ __device__ __forceinline__ void forward_step(const SigGeometry& sg, const SigSha
         __syncthreads();
     }
     const T* x1 = xc + W;
+    int n_first = 1;
+    if constexpr (kVec4<T, WT>) {
+        if (vec4) {  // (top level in shared memory)
+            uint32_t v = threadIdx.x;
+            for (int n = 1; n <= nmax; ++n) {
+                const T* prev = chain(sg, sh.Tf, n, n - 1);
+                float4* Sn = reinterpret_cast<float4*>(S + G.db[n]);
+                const uint32_t groups = G.pw[n] / 4;
+                for (; v < groups; v += blockDim.x) {
+                    const uint32_t u = 4 * v, q = u / WT, a = u % WT;
+                    const T pq = n == 1 ? s0 : prev[q];
+                    const float4 xv = *reinterpret_cast<const float4*>(x1 + a);
+                    float4 sv = Sn[v];
+                    sv.x = fmaf(pq, xv.x, sv.x);
+                    sv.y = fmaf(pq, xv.y, sv.y);
+                    sv.z = fmaf(pq, xv.z, sv.z);
+                    sv.w = fmaf(pq, xv.w, sv.w);
+                    Sn[v] = sv;
+                }
+                v -= groups;
+            }
+            n_first = nmax + 1;
+        }
+    }
     uint32_t v = threadIdx.x;
-    for (int n = 1; n <= nmax; ++n) {
+    for (int n = n_first; n <= nmax; ++n) {
         const uint32_t wn = G.pw[n];
         T* Sn = n == G.depth ? sh.top : S + G.db[n];
         const T* prev = chain(sg, sh.Tf, n, n - 1);
@@ -442,9 +502,18 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? 2 : 1)) k_signature(SigGe
     SigShared<T> sh;
     T* q = reinterpret_cast<T*>(smem_raw);
     T* p = gws ? gws + blockIdx.x * gws_stride : q;
+    // the FP32 four-coefficient forward step wants S + 1, Tf + choff[1] and the
+    // scaled increments on 16-byte boundaries (kVec4; the host adds slack)
+    bool vec4 = false;
+    if constexpr (kVec4<T, WT>) vec4 = gws == nullptr && !top_global;
+    auto align4 = [&](uint32_t off) {  // elements to skip so that p + off is 16-byte aligned
+        return vec4 ? static_cast<uint32_t>((4u - (static_cast<uint32_t>(p - q) + off) % 4u) % 4u) : 0u;
+    };
+    p += align4(1);
     sh.S = p;
     sh.top = p + lo;
     p += held;
+    p += align4(sg.choff[1]);
     sh.Tf = p;
     p += sg.chain_total;
     if (bwd) {
@@ -456,6 +525,7 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? 2 : 1)) k_signature(SigGe
         sh.G = sh.Tb = nullptr;
     }
     if (gws) p = q;
+    p += align4(0);
     sh.xcs = (D + 1) * W;
     sh.xc = p;
     p += 2 * sh.xcs;
@@ -500,7 +570,7 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? 2 : 1)) k_signature(SigGe
             for (int64_t k = 0; k < len; ++k) {
                 const T x_next = xv;
                 if (k + 2 < len) xv = load_increment(sg, xin, k + 2);
-                forward_step<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k + 1), x_next, nmax, top_global);
+                forward_step<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k + 1), x_next, nmax, top_global, vec4);
             }
             if (sig && !(mode & kLoadFinal)) {
                 T* dst = sig + b * sig_stride;
@@ -607,6 +677,7 @@ size_t sig_smem_bytes(const SigGeometry& sg, int threads, bool bwd, bool residen
     const size_t D = sg.g.depth, W = sg.g.width;
     size_t n = 2 * (D + 1) * W + (D + 1) + (D + 2) + threads;
     if (resident) n += sig_state_elems(sg, bwd, top_global);
+    if (std::is_same<T, float>::value) n += 12;  // alignment padding of the FP32 four-coefficient step
     return n * sizeof(T);
 }
 
