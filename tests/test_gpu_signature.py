@@ -251,6 +251,28 @@ def test_every_schedule_matches_oracle(orc, schedule, ragged):
 
 
 
+
+@pytest.mark.parametrize("schedule", [512 | (1 << 14), 256 | (3 << 14), 128 | (1 << 14) | (512 << 16)])
+def test_two_launch_large_state_matches_oracle(orc, schedule):
+    """W6 D6 FP64 does not fit shared memory: under a two-launch schedule the
+    forward launch keeps its state on chip (top level in global memory) and
+    the reverse launch runs in the global workspace -- with 2 x 152 CTAs of
+    half size when that workspace fits in L2 -- against the oracle."""
+    W, D, B, L = 6, 6, 3, 6
+    rng = np.random.default_rng(schedule & 0xFFFF)
+    incr = rng.normal(0, 1 / np.sqrt(L), (B * L, W))
+    dim = O.tensor_dim(W, D)
+    ell = rng.uniform(-1, 1, (B, dim))
+    basis = pkg.TensorBasis(W, D)
+    sig = torch.full((B, dim), float("nan"), dtype=torch.float64, device="cuda")
+    grad = torch.full((B * L, W), float("nan"), dtype=torch.float64, device="cuda")
+    err = pkg.signature(pkg.GB300Strategy(torch.float64), None, dev(incr), basis, B, length=L, out=sig,
+                        seed=dev(ell), grad=grad, schedule=schedule)
+    assert err, err.message
+    esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
+    assert_close(host(sig), esig, TOL_F64, f"W6 D6 signature, schedule {schedule}")
+    assert_close(host(grad), egrad, TOL_F64, f"W6 D6 gradient, schedule {schedule}")
+
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 @pytest.mark.parametrize("W,D,B,L,chunk", [(5, 5, 7, 16, 0), (5, 5, 7, 16, 3), (3, 4, 10, 9, 1), (4, 4, 5, 8, 64),
                                            (2, 6, 9, 12, 4)])
