@@ -483,8 +483,11 @@ __device__ __forceinline__ void backward_step(const SigGeometry& sg, const SigSh
 // the state and chain arrays of CTA i live in gws + i*gws_stride (global
 // memory, L2-resident at the grid sizes used) and only the increments,
 // 1/m and the partials stay in shared memory.
+// Registers: at most 64 per thread for FP64 (two 512-thread blocks per SM;
+// the fastest measured), 40 for FP32, whose small states fit more CTAs per SM
+// than 64 registers allow (ragged W8 D4 FP32: 29.3 -> 28.3 ms).
 template <typename T, int WT, int MAXT>
-__global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? 2 : 1)) k_signature(SigGeometry sg, const T* __restrict__ incr, PathBatch paths,
+__global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? (sizeof(T) == 4 ? 3 : 2) : 1)) k_signature(SigGeometry sg, const T* __restrict__ incr, PathBatch paths,
                                                     T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
                                                     T* grad, int mode, T* gws, int64_t gws_stride) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
