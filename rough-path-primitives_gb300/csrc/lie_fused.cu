@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256) k_log_to_lie(Geometry G, CsrDevice m, TAr
         if (!st.commit(G.fault)) return;
         intermediate_one(G, IntermediateKind::Log, s_log, lo, hi, X, none);
         __syncthreads();
-        sell_rows<Scale>(m, s_log + G.db[lo], out + b * out_stride, out_size, alpha);
+        sell_rows<Scale, true>(m, s_log + G.db[lo], out + b * out_stride, out_size, alpha);  // t2l: long rows
         bulk_stage_reuse();
     }
 }
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(256) k_lie_exp(Geometry G, CsrDevice m, const 
         if (fm) M = {mult.at(b), mult.lo, imin(mult.hi, G.depth)};
         for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) s_x[i] = T(0);
         if (!st.commit(G.fault)) return;
-        sell_rows<Scale>(m, l, s_x + G.db[lo], static_cast<int64_t>(view), alpha);
+        sell_rows<Scale, false>(m, l, s_x + G.db[lo], static_cast<int64_t>(view), alpha);  // l2t: short rows
         __syncthreads();
         const Opnd<T> X{s_x, imax(1, lo), hi};
         intermediate_one(G, fm ? IntermediateKind::FMExp : IntermediateKind::Exp, s_o, out.lo, ohi, X, M);

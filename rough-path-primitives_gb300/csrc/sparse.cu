@@ -20,7 +20,7 @@
 namespace rpp_gb {
 namespace {
 
-template <typename T, bool Scale>
+template <typename T, bool Scale, bool Unroll>
 __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_stride, int64_t out_size,
                                               const T* arg, int64_t arg_stride, int64_t arg_size,
                                               int64_t batch, T alpha, int staged) {
@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(256) k_spmm(CsrDevice m, T* out, int64_t out_s
             x = st.add_span(s_arg, x, 0, static_cast<uint32_t>(arg_size));
             if (!st.commit(m.fault)) return;
         }
-        sell_rows<Scale>(m, x, y, out_size, alpha);
+        sell_rows<Scale, Unroll>(m, x, y, out_size, alpha);
         if (staged) bulk_stage_reuse();
     }
 }
@@ -63,8 +63,11 @@ cudaError_t launch_spmm(const CsrDevice& m, const DeviceInfo& dev, cudaStream_t 
                                       static_cast<T>(alpha), staged);
         return cudaGetLastError();
     };
-    if (static_cast<T>(alpha) == T(1)) return run(std::integral_constant<decltype(&k_spmm<T, false>), &k_spmm<T, false>>{});
-    return run(std::integral_constant<decltype(&k_spmm<T, true>), &k_spmm<T, true>>{});
+    const bool one = static_cast<T>(alpha) == T(1), longrows = m.nnz >= 8 * m.rows;  // (sell.cuh)
+    if (one && longrows) return run(std::integral_constant<decltype(&k_spmm<T, false, true>), &k_spmm<T, false, true>>{});
+    if (one) return run(std::integral_constant<decltype(&k_spmm<T, false, false>), &k_spmm<T, false, false>>{});
+    if (longrows) return run(std::integral_constant<decltype(&k_spmm<T, true, true>), &k_spmm<T, true, true>>{});
+    return run(std::integral_constant<decltype(&k_spmm<T, true, false>), &k_spmm<T, true, false>>{});
 }
 
 template cudaError_t launch_spmm<float>(const CsrDevice&, const DeviceInfo&, cudaStream_t, float*, int64_t,
