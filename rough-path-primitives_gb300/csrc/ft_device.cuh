@@ -65,9 +65,10 @@ __device__ void product_levels(const Geometry& G, T* dst, int lo, int hi, const 
         const uint32_t base = G.db[n];
         const bool has_add = add.p != nullptr && add.lo <= n && n <= add.hi;
         for (uint32_t i = threadIdx.x; i < size; i += blockDim.x) {
+            const T av = has_add ? add.p[base + i] : T(0);  // issued before the sum's loads
             T val = split_sum(G, L, R, n, i);
             if constexpr (Scale) val *= beta;
-            if (has_add) val = fma(alpha, add.p[base + i], val);
+            if (has_add) val = fma(alpha, av, val);
             dst[base + i] = val;
         }
         if (sync) __syncthreads();
