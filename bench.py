@@ -753,6 +753,7 @@ def main():
                                 "two_launches": bool(tuned_threads & (1 << 14)),
                                 "forward_top_level_in_global": bool(tuned_threads & (1 << 15)),
                                 "reverse_threads_per_cta": ((tuned_threads >> 16) & 1023) or (tuned_threads & 1023),
+                                "cotangent_in_global": bool(tuned_threads & (1 << 26)),
                                 "chosen_by": "rpp_gb_signature_tune" if pinned is None else "--schedule"}},
         "roofline": {"bound": "fp64_fma", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": (achieved / fp64_peak) if fp64_peak else None,

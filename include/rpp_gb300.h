@@ -419,7 +419,10 @@ int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream strea
  * in bits 10-13, bit 14 set for the two-launch form, bit 15 set when its
  * forward launch keeps the top level in the output row in global memory, and
  * for the two-launch form the reverse launch's own CTA size in bits 16-25
- * (0: the same as the forward launch's).  A two-launch winner is refined by
+ * (0: the same as the forward launch's), and bit 26 set when the launch with
+ * the reverse pass keeps the cotangent arrays in a global workspace (the
+ * state and forward chains stay in shared memory; more CTAs per SM for deep
+ * narrow shapes).  A two-launch winner is refined by
  * timing other reverse sizes, then other forward sizes. */
 int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
                           const void* incr, const int64_t* offsets, int64_t length, int64_t batch,

@@ -347,7 +347,7 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         return rc;
     static const int sizes[] = {128, 192, 256, 320, 384, 512};
     static const int caps[] = {0, 3, 2};
-    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 5];
+    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 8];
     int ncand = 0;
     for (int c : caps)
         for (int t : sizes) candidates[ncand++] = t | (c << 10);
@@ -357,6 +357,15 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         for (int t : sizes) {
             candidates[ncand++] = t | rpp_gb::kScheduleSplit;
             candidates[ncand++] = t | rpp_gb::kScheduleSplit | rpp_gb::kScheduleForwardTopGlobal;
+        }
+    // a reverse pass with the cotangent arrays in a global workspace (fused
+    // form, and the two-launch form's reverse launch)
+    if (seed && grad)
+        for (int t : {256, 512}) {
+            candidates[ncand++] = t | rpp_gb::kScheduleCotangentGlobal;
+            if (sig)
+                candidates[ncand++] = t | rpp_gb::kScheduleSplit | rpp_gb::kScheduleForwardTopGlobal |
+                                      rpp_gb::kScheduleCotangentGlobal;
         }
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
@@ -396,7 +405,7 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
     if (best & rpp_gb::kScheduleSplit) {
         constexpr int sh = rpp_gb::kScheduleReverseShift;
         const int fwd = best & 1023;
-        const int flags = best & ((1 << sh) - 1) & ~1023;
+        const int flags = best & ~1023 & ~(1023 << sh);
         for (int t : sizes)
             if (t != fwd) try_candidate(flags | fwd | (t << sh));
         const int rev = (best >> sh) & 1023 ? (best >> sh) & 1023 : fwd;

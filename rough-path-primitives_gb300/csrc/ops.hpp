@@ -174,6 +174,10 @@ struct PathBatch {
 constexpr int kScheduleSplit = 1 << 14;
 constexpr int kScheduleForwardTopGlobal = 1 << 15;
 constexpr int kScheduleReverseShift = 16;
+// kScheduleCotangentGlobal: a launch with a reverse pass keeps the state and
+// the forward chains in shared memory and the cotangent level and chains in
+// a per-CTA global workspace (L2-resident), so more CTAs fit per SM.
+constexpr int kScheduleCotangentGlobal = 1 << 26;
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,

@@ -62,7 +62,7 @@ struct SigGeometry {
 // less than one level (W2 D12 FP64: 229 KB, 196 KB without its top) still
 // runs resident.  Level D is only ever updated by the thread that owns the
 // coefficient, so no barrier orders these accesses.
-enum SigMode : int { kForward = 1, kBackward = 2, kLoadFinal = 4, kTopLevel = 8, kTopGlobal = 16 };
+enum SigMode : int { kForward = 1, kBackward = 2, kLoadFinal = 4, kTopLevel = 8, kTopGlobal = 16, kCotGlobal = 32 };
 
 template <typename T>
 struct SigShared {
@@ -504,7 +504,10 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? (sizeof(T) == 4 ? 3 : 2) 
 
     SigShared<T> sh;
     T* q = reinterpret_cast<T*>(smem_raw);
-    T* p = gws ? gws + blockIdx.x * gws_stride : q;
+    // kCotGlobal: S and the forward chains in shared memory, the cotangent
+    // level and chains in this CTA's slice of the global workspace
+    const bool cot_global = (mode & kCotGlobal) && bwd && gws;
+    T* p = (gws && !cot_global) ? gws + blockIdx.x * gws_stride : q;
     // the FP32 four-coefficient forward step wants S + 1, Tf + choff[1] and the
     // scaled increments on 16-byte boundaries (kVec4; the host adds slack)
     bool vec4 = false;
@@ -520,14 +523,16 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? (sizeof(T) == 4 ? 3 : 2) 
     sh.Tf = p;
     p += sg.chain_total;
     if (bwd) {
-        sh.G = p;
-        p += lo;
-        sh.Tb = p;
-        p += sg.chain_total;
+        T* g = cot_global ? gws + blockIdx.x * gws_stride : p;
+        sh.G = g;
+        g += lo;
+        sh.Tb = g;
+        g += sg.chain_total;
+        if (!cot_global) p = g;
     } else {
         sh.G = sh.Tb = nullptr;
     }
-    if (gws) p = q;
+    if (gws && !cot_global) p = q;
     p += align4(0);
     sh.xcs = (D + 1) * W;
     sh.xc = p;
@@ -728,6 +733,35 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
         mode |= kTopGlobal;
         smem = sig_smem_bytes<T>(sg, threads, bwd, true, true);
     }
+    if (bwd && (schedule & kScheduleCotangentGlobal)) {
+        // cotangent level and chains in a stream-ordered global workspace (one
+        // slice per CTA, L2-resident: 30 MB for two CTAs per SM at W2 D12
+        // FP64), state and forward chains resident: at W2 D12 FP64 the reverse
+        // launch drops from 196 KB to 98 KB of shared memory per CTA, two CTAs
+        // fit per SM, and fwd+bwd runs 49 079 -> 63 370 paths/s (with a
+        // 512-thread reverse launch); at W5 D5 it is slower (105 748 -> 103 799)
+        mode |= kCotGlobal;
+        size_t hsmem = sig_smem_bytes<T>(sg, threads, false, true, mode & kTopGlobal);
+        if (hsmem + 64 > optin && !(mode & kTopGlobal)) {  // the top level to global memory too
+            mode |= kTopGlobal;
+            hsmem = sig_smem_bytes<T>(sg, threads, false, true, true);
+        }
+        if (hsmem + 64 > optin) return cudaErrorInvalidConfiguration;
+        constexpr auto kernel = k_signature<T, WT, kResidentMaxThreads>;
+        cudaError_t err = allow_large_smem<kernel>(dev);
+        if (err != cudaSuccess) return err;
+        if (threads < sg.g.depth * sg.g.width || threads < sg.g.width) return cudaErrorInvalidConfiguration;
+        dim3 grid;
+        if ((err = batch_grid(kernel, dev, threads, hsmem, paths.batch, grid)) != cudaSuccess) return err;
+        const int64_t stride = static_cast<int64_t>((sg.g.db[sg.g.depth] + sg.chain_total + 31) / 32 * 32);
+        T* ws = nullptr;
+        err = cudaMallocAsync(reinterpret_cast<void**>(&ws), static_cast<size_t>(grid.x) * stride * sizeof(T), s);
+        if (err != cudaSuccess) return err;
+        kernel<<<grid, threads, hsmem, s>>>(sg, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, ws, stride);
+        err = cudaGetLastError();
+        cudaError_t ferr = cudaFreeAsync(ws, s);
+        return err != cudaSuccess ? err : ferr;
+    }
     if (smem + 64 <= optin) {
         constexpr auto kernel = k_signature<T, WT, kResidentMaxThreads>;
         cudaError_t err = allow_large_smem<kernel>(dev);
@@ -798,8 +832,9 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
     int rev_threads = threads;
     if (split) {
         const int rev = (threads >> kScheduleReverseShift) & 1023;
+        const int cot = threads & kScheduleCotangentGlobal;
         threads &= (1 << 14) - 1;  // CTA size and cap
-        rev_threads = rev > 0 ? (threads & ~1023) | rev : threads;
+        rev_threads = (rev > 0 ? (threads & ~1023) | rev : threads) | cot;
     }
     int mode = 0;
     if (forward) {

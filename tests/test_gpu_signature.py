@@ -205,11 +205,12 @@ def test_autotuner_records_schedule_and_keeps_parity(orc):
     assert err, err.message
     # schedule: threads per CTA in bits 0-9, CTA-per-SM cap in bits 10-13,
     # bit 14 for the two-launch form (bit 15: its forward top level in global
-    # memory; bits 16-25: its reverse launch's own CTA size)
+    # memory; bits 16-25: its reverse launch's own CTA size), bit 26 for the
+    # cotangent arrays in a global workspace
     sizes = (128, 192, 256, 320, 384, 512)
     assert (threads & 1023) in sizes and ((threads >> 10) & 15) in (0, 2, 3)
-    assert (threads >> 26) == 0 and ((threads >> 16) & 1023) in (0,) + sizes
-    assert (threads >> 16) == 0 or threads & (1 << 14)
+    assert (threads >> 27) == 0 and ((threads >> 16) & 1023) in (0,) + sizes
+    assert ((threads >> 16) & 1023) == 0 or threads & (1 << 14)
     assert ms > 0
     esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
     assert_close(host(sig), esig, TOL_F64, "tuned signature")
@@ -220,7 +221,8 @@ def test_autotuner_records_schedule_and_keeps_parity(orc):
 
 @pytest.mark.parametrize("schedule", [128, 256, 128 | (3 << 10), 192 | (2 << 10), 128 | (1 << 14),
                                       256 | (1 << 14), 128 | (3 << 14), 320 | (3 << 14),
-                                      128 | (1 << 14) | (256 << 16), 256 | (3 << 14) | (128 << 16)])
+                                      128 | (1 << 14) | (256 << 16), 256 | (3 << 14) | (128 << 16),
+                                      256 | (1 << 26), 128 | (3 << 14) | (1 << 26), 128 | (3 << 14) | (512 << 16) | (1 << 26)])
 @pytest.mark.parametrize("ragged", [False, True])
 def test_every_schedule_matches_oracle(orc, schedule, ragged):
     """Each schedule the autotuner can pick (CTA size, a cap on CTAs per SM,
@@ -252,7 +254,8 @@ def test_every_schedule_matches_oracle(orc, schedule, ragged):
 
 
 
-@pytest.mark.parametrize("schedule", [512 | (1 << 14), 256 | (3 << 14), 128 | (1 << 14) | (512 << 16)])
+@pytest.mark.parametrize("schedule", [512 | (1 << 14), 256 | (3 << 14), 128 | (1 << 14) | (512 << 16),
+                                      512 | (1 << 14) | (1 << 26), 256 | (1 << 26)])
 def test_two_launch_large_state_matches_oracle(orc, schedule):
     """W6 D6 FP64 does not fit shared memory: under a two-launch schedule the
     forward launch keeps its state on chip (top level in global memory) and
@@ -272,6 +275,27 @@ def test_two_launch_large_state_matches_oracle(orc, schedule):
     esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
     assert_close(host(sig), esig, TOL_F64, f"W6 D6 signature, schedule {schedule}")
     assert_close(host(grad), egrad, TOL_F64, f"W6 D6 gradient, schedule {schedule}")
+
+
+@pytest.mark.parametrize("schedule", [256 | (3 << 14) | (512 << 16) | (1 << 26), 512 | (1 << 26), 256 | (3 << 14)])
+def test_deep_narrow_cotangent_workspace_matches_oracle(orc, schedule):
+    """W2 D12 FP64 (196 KB of reverse state): the cotangent level and chains in
+    the global workspace, state and forward chains resident, two CTAs per SM
+    -- against the oracle, fused and two-launch."""
+    W, D, B, L = 2, 12, 3, 10
+    rng = np.random.default_rng(schedule & 0xFFFFF)
+    incr = rng.normal(0, 1 / np.sqrt(L), (B * L, W))
+    dim = O.tensor_dim(W, D)
+    ell = rng.uniform(-1, 1, (B, dim))
+    basis = pkg.TensorBasis(W, D)
+    sig = torch.full((B, dim), float("nan"), dtype=torch.float64, device="cuda")
+    grad = torch.full((B * L, W), float("nan"), dtype=torch.float64, device="cuda")
+    err = pkg.signature(pkg.GB300Strategy(torch.float64), None, dev(incr), basis, B, length=L, out=sig,
+                        seed=dev(ell), grad=grad, schedule=schedule)
+    assert err, err.message
+    esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
+    assert_close(host(sig), esig, TOL_F64, f"W2 D12 signature, schedule {schedule}")
+    assert_close(host(grad), egrad, TOL_F64, f"W2 D12 gradient, schedule {schedule}")
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 @pytest.mark.parametrize("W,D,B,L,chunk", [(5, 5, 7, 16, 0), (5, 5, 7, 16, 3), (3, 4, 10, 9, 1), (4, 4, 5, 8, 64),
