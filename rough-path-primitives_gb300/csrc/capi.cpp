@@ -347,7 +347,7 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         return rc;
     static const int sizes[] = {128, 192, 256, 320, 384, 512};
     static const int caps[] = {0, 3, 2};
-    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 8];
+    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 8 + 8];
     int ncand = 0;
     for (int c : caps)
         for (int t : sizes) candidates[ncand++] = t | (c << 10);
@@ -363,9 +363,10 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
     if (seed && grad)
         for (int t : {256, 512}) {
             candidates[ncand++] = t | rpp_gb::kScheduleCotangentGlobal;
-            if (sig)
-                candidates[ncand++] = t | rpp_gb::kScheduleSplit | rpp_gb::kScheduleForwardTopGlobal |
-                                      rpp_gb::kScheduleCotangentGlobal;
+            if (sig)  // the two-launch form: this forward size with a 512-thread reverse launch too
+                for (int rev : {0, 512})
+                    candidates[ncand++] = t | rpp_gb::kScheduleSplit | rpp_gb::kScheduleForwardTopGlobal |
+                                          rpp_gb::kScheduleCotangentGlobal | (rev << rpp_gb::kScheduleReverseShift);
         }
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
