@@ -277,8 +277,9 @@ def test_two_launch_large_state_matches_oracle(orc, schedule):
     assert_close(host(grad), egrad, TOL_F64, f"W6 D6 gradient, schedule {schedule}")
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 @pytest.mark.parametrize("schedule", [256 | (3 << 14) | (512 << 16) | (1 << 26), 512 | (1 << 26), 256 | (3 << 14)])
-def test_deep_narrow_cotangent_workspace_matches_oracle(orc, schedule):
+def test_deep_narrow_cotangent_workspace_matches_oracle(orc, schedule, dtype):
     """W2 D12 FP64 (196 KB of reverse state): the cotangent level and chains in
     the global workspace, state and forward chains resident, two CTAs per SM
     -- against the oracle, fused and two-launch."""
@@ -288,14 +289,15 @@ def test_deep_narrow_cotangent_workspace_matches_oracle(orc, schedule):
     dim = O.tensor_dim(W, D)
     ell = rng.uniform(-1, 1, (B, dim))
     basis = pkg.TensorBasis(W, D)
-    sig = torch.full((B, dim), float("nan"), dtype=torch.float64, device="cuda")
-    grad = torch.full((B * L, W), float("nan"), dtype=torch.float64, device="cuda")
-    err = pkg.signature(pkg.GB300Strategy(torch.float64), None, dev(incr), basis, B, length=L, out=sig,
-                        seed=dev(ell), grad=grad, schedule=schedule)
+    sig = torch.full((B, dim), float("nan"), dtype=dtype, device="cuda")
+    grad = torch.full((B * L, W), float("nan"), dtype=dtype, device="cuda")
+    err = pkg.signature(pkg.GB300Strategy(dtype), None, dev(incr, dtype), basis, B, length=L, out=sig,
+                        seed=dev(ell, dtype), grad=grad, schedule=schedule)
     assert err, err.message
     esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
-    assert_close(host(sig), esig, TOL_F64, f"W2 D12 signature, schedule {schedule}")
-    assert_close(host(grad), egrad, TOL_F64, f"W2 D12 gradient, schedule {schedule}")
+    tol = TOL_F64 if dtype == torch.float64 else TOL_F32
+    assert_close(host(sig), esig, tol, f"W2 D12 signature, schedule {schedule}")
+    assert_close(host(grad), egrad, tol, f"W2 D12 gradient, schedule {schedule}")
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 @pytest.mark.parametrize("W,D,B,L,chunk", [(5, 5, 7, 16, 0), (5, 5, 7, 16, 3), (3, 4, 10, 9, 1), (4, 4, 5, 8, 64),
