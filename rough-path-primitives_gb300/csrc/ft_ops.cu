@@ -149,7 +149,10 @@ __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> o
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     T* sm = reinterpret_cast<T*>(smem_raw + kBulkHeader);
     const uint32_t pd = staged_elems<T>(G.dim);
-    T* s_part = sm + (staged ? 2 * pd : 0);  // one partial per thread
+    // staged: 0 = nothing, 1 = both operands, 2 = the op only (arg read
+    // through L1/L2 -- in both mappings a warp's lanes read consecutive
+    // argument coefficients)
+    T* s_part = sm + (staged == 1 ? 2 * pd : staged == 2 ? pd : 0);  // one partial per thread
     uint32_t phase = 0;
     if (staged) bulk_stage_init(bar);
     const int D = G.depth;
@@ -162,7 +165,7 @@ __global__ void __launch_bounds__(256) k_adjoint(Geometry G, int left, TArg<T> o
         if (staged) {
             BulkStage<T> st(bar, phase);
             P = st.add(sm, P, op.lo, phi, G);
-            A = st.add(sm + pd, A, arg.lo, ahi, G);
+            if (staged == 1) A = st.add(sm + pd, A, arg.lo, ahi, G);
             if (!st.commit(G.fault)) return;
         }
         for (int m = out.lo; m <= ohi; ++m) {
@@ -424,10 +427,23 @@ cudaError_t launch_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_
     constexpr auto kernel = k_adjoint<T>;
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
-    const size_t smem_need = 2 * static_cast<size_t>(staged_elems<T>(g.dim)) * sizeof(T);
+    // Both operands staged while that leaves two or more CTAs per SM; when it
+    // would leave one (W2 D12 FP64: 131 KB), the op alone, for three CTAs per
+    // SM (W2 D12, batch 16 384: ft_adj_lmul 4.46 -> 3.90 ms, ft_adj_rmul 4.56 ->
+    // 4.15 ms; at W16 D3, 70 KB for both and three CTAs per SM, op-only staging
+    // measured slower).
+    const size_t one = static_cast<size_t>(staged_elems<T>(g.dim)) * sizeof(T);
     const size_t part = kBulkHeader + 256 * sizeof(T);  // the mbarrier and one partial per thread
-    const int staged = smem_need + part <= kStageLimit && smem_need + part <= static_cast<size_t>(dev.max_smem_optin);
-    const size_t smem = (staged ? smem_need : 0) + part;
+    const size_t limit = std::min(kStageLimit, static_cast<size_t>(dev.max_smem_optin));
+    int per_sm = 0;
+    if ((err = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev.device)) != cudaSuccess)
+        return err;
+    int staged = 0;
+    if (2 * one + part <= limit && 2 * (2 * one + part + 1024) <= static_cast<size_t>(per_sm))
+        staged = 1;
+    else if (one + part <= limit)
+        staged = 2;
+    const size_t smem = (staged == 1 ? 2 * one : staged == 2 ? one : 0) + part;
     const int threads = threads_for(g.pw[g.depth]);
     dim3 grid;
     if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;

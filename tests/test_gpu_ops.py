@@ -168,7 +168,8 @@ def test_antipode_bit_exact(ops_golden, dtype, signed):
 
 
 # Larger random cases against the oracle, including the benchmark shapes.
-RANDOM_SHAPES = [(4, 4, 64), (5, 5, 8), (2, 8, 8), (8, 3, 8), (16, 3, 2), (1, 5, 4), (3, 0, 4), (6, 4, 3)]
+RANDOM_SHAPES = [(4, 4, 64), (5, 5, 8), (2, 8, 8), (8, 3, 8), (16, 3, 2), (1, 5, 4), (3, 0, 4), (6, 4, 3),
+                 (2, 12, 3)]  # (W2 D12: the adjoints stage the op only)
 
 
 @pytest.mark.parametrize("W,D,n", RANDOM_SHAPES)
