@@ -486,7 +486,10 @@ __device__ __forceinline__ void backward_step(const SigGeometry& sg, const SigSh
 // Registers: at most 64 per thread for FP64 (two 512-thread blocks per SM;
 // the fastest measured), 40 for FP32, whose small states fit more CTAs per SM
 // than 64 registers allow (ragged W8 D4 FP32: 29.3 -> 28.3 ms).
-template <typename T, int WT, int MAXT>
+// COT: the cotangent arrays may live in the global workspace (kCotGlobal) --
+// a separate instantiation, so that the other kernels' code is what it was
+// without that option (it cost W16 D3 2.6 % when it was a run-time choice).
+template <typename T, int WT, int MAXT, bool COT = false>
 __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? (sizeof(T) == 4 ? 3 : 2) : 1)) k_signature(SigGeometry sg, const T* __restrict__ incr, PathBatch paths,
                                                     T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
                                                     T* grad, int mode, T* gws, int64_t gws_stride) {
@@ -506,7 +509,7 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? (sizeof(T) == 4 ? 3 : 2) 
     T* q = reinterpret_cast<T*>(smem_raw);
     // kCotGlobal: S and the forward chains in shared memory, the cotangent
     // level and chains in this CTA's slice of the global workspace
-    const bool cot_global = (mode & kCotGlobal) && bwd && gws;
+    const bool cot_global = COT && (mode & kCotGlobal) && bwd && gws;
     T* p = (gws && !cot_global) ? gws + blockIdx.x * gws_stride : q;
     // the FP32 four-coefficient forward step wants S + 1, Tf + choff[1] and the
     // scaled increments on 16-byte boundaries (kVec4; the host adds slack)
@@ -747,7 +750,7 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
             hsmem = sig_smem_bytes<T>(sg, threads, false, true, true);
         }
         if (hsmem + 64 > optin) return cudaErrorInvalidConfiguration;
-        constexpr auto kernel = k_signature<T, WT, kResidentMaxThreads>;
+        constexpr auto kernel = k_signature<T, WT, kResidentMaxThreads, true>;
         cudaError_t err = allow_large_smem<kernel>(dev);
         if (err != cudaSuccess) return err;
         if (threads < sg.g.depth * sg.g.width || threads < sg.g.width) return cudaErrorInvalidConfiguration;
