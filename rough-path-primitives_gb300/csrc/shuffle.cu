@@ -221,11 +221,13 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
 //     OP[ob(a, m) + u] * ARG[ab(a, m) + merge(w, u, M)]
 // (W^k terms; one when m = 0), so the walk that places w's and u_hi's
 // letters is paid once per W^k FMAs.  Items are visited op degree first,
-// highest degree (largest items) first, then letter, mask and u_hi, so that
-// lanes taking every 32nd item get the large items first and balance.  A cursor walks the items in that order; lanes of a
-// warp take every 32nd item, a single thread takes them all.  Skipping ahead
-// costs one Gosper step per mask passed, so each lane pays O(#masks) integer
-// work besides its share of the items.
+// highest degree (largest items) first, then mask, u_hi and letter, so that
+// lanes taking every 32nd item get the large items first and balance.  A
+// cursor walks the items in that order; lanes of a warp take every 32nd item,
+// a single thread takes them all.  Skipping ahead costs one Gosper step per
+// mask passed; with the letter innermost, a lane of the left adjoint passes
+// 32/W (mask, u_hi) pairs per item instead of 32 (letter outside the mask,
+// every mask of a low degree one pair).
 struct AdjItems {
     int kind;
     int nw;       // letters of the output word w (after the rmul prefix)
@@ -249,10 +251,7 @@ struct AdjItems {
             M = ripple | (((ripple ^ M) >> 2) >> (__ffs(M) - 1));
             return true;
         }
-        if (++a >= a1) {
-            a = a0;
-            if (--m < mlo) return false;
-        }
+        if (--m < mlo) return false;
         start_degree(G);
         return true;
     }
@@ -267,7 +266,14 @@ struct AdjItems {
         }
     }
     __device__ void advance(const Geometry& G, uint32_t k) {
-        uh += k;
+        // k items on: the letter is the innermost digit (a1 - a0 = 1 or W)
+        uint32_t carry = k;
+        if (a1 - a0 > 1) {
+            uint32_t r;
+            G.divw.divmod(static_cast<uint32_t>(a - a0) + k, carry, r);
+            a = a0 + static_cast<int>(r);
+        }
+        uh += carry;
         while (uh >= nhi) {
             uh -= nhi;
             if (!next_mask(G)) {
