@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <type_traits>
 
 #include "bulk_stage.cuh"
 #include "launch_util.cuh"
@@ -142,7 +143,9 @@ __device__ T shuffle_word(const Geometry& G, int m, uint32_t v, int e, uint32_t 
     return acc;
 }
 
-template <typename T, int MAXD>
+// Scale: beta != 1, multiplied in per coefficient (a compile-time choice:
+// as a run-time select the multiply ran for every coefficient).
+template <typename T, int MAXD, bool Scale>
 __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, TArg<T> out, TArg<T> add, TArg<T> lhs,
                                                         TArg<T> rhs, int64_t batch, T alpha, T beta, int staged,
                                                         ShuffleOrder ord) {
@@ -190,11 +193,11 @@ __global__ void __launch_bounds__(256) k_shuffle_product(Geometry G, int kind, T
                         const uint32_t tail = G.pw[n - 1];
                         const uint32_t a = j / tail, v = j - a * tail;
                         val = shuffle_word<T, MAXD>(G, n - 1, v, 1, a, L, lhs.lo, lhi, R, rhs.lo, rhi);
-                        if (beta != T(1)) val *= beta;
+                        if constexpr (Scale) val *= beta;
                     }
                 } else {
                     val = shuffle_word<T, MAXD>(G, n, j, 0, 0u, L, lhs.lo, lhi, R, rhs.lo, rhi);
-                    if (beta != T(1)) val *= beta;
+                    if constexpr (Scale) val *= beta;
                     if (kind == static_cast<int>(ShuffleKind::InplaceFma)) {
                         val = fma(alpha, o[G.db[n] + j], val);
                     } else if (kind == static_cast<int>(ShuffleKind::Fma) && A && add.has(n)) {
@@ -536,7 +539,10 @@ __device__ T adjoint_coeff_seq_left(const Geometry& G, int n, uint32_t w, const 
     return acc;
 }
 
-template <typename T>
+// Scale: beta != 1 (compile time; as a run-time select the FP64 multiply ran
+// for every output coefficient: 7 % of the DFMA count of left_hs_adj_lmul at
+// W5 D5).
+template <typename T, bool Scale>
 __global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind, TArg<T> out, TArg<T> op,
                                                         TArg<T> arg, int64_t batch, T beta, int staged,
                                                         ShuffleOrder ord) {
@@ -576,7 +582,7 @@ __global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind
                 locate(ord, t, n, j);
                 T acc = adjoint_coeff<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi, lane, 32);
                 acc = warp_reduce(acc);
-                if (lane == 0) o[G.db[n] + j] = beta == T(1) ? acc : beta * acc;
+                if (lane == 0) o[G.db[n] + j] = Scale ? beta * acc : acc;
             } else {
                 const uint32_t k = nwarp + (t - nwarp) * 32 + lane;
                 if (k < total) {
@@ -586,7 +592,7 @@ __global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind
                     const T acc = kind == static_cast<int>(ShuffleAdjKind::HalfL)
                                       ? adjoint_coeff_seq_left<T>(G, n, j, P, op.lo, ohi, A, arg.lo, ahi)
                                       : adjoint_coeff_seq<T>(G, kind, n, j, P, op.lo, ohi, A, arg.lo, ahi);
-                    o[G.db[n] + j] = beta == T(1) ? acc : beta * acc;
+                    o[G.db[n] + j] = Scale ? beta * acc : acc;
                 }
             }
         }
@@ -705,9 +711,9 @@ cudaError_t launch_shuffle_product(const Geometry& g, const DeviceInfo& dev, cud
     size_t smem;
     dim3 grid;
     cudaError_t err;
-#define RPP_GB_SHUFFLE_FWD(MAXD)                                                                           \
+#define RPP_GB_SHUFFLE_FWD(MAXD, SCALE)                                                                    \
     {                                                                                                      \
-        constexpr auto kernel = k_shuffle_product<T, MAXD>;                                                \
+        constexpr auto kernel = k_shuffle_product<T, MAXD, SCALE>;                                         \
         if ((err = allow_large_smem<kernel>(dev)) != cudaSuccess) return err;                              \
         if ((err = shuffle_launch_shape(kernel, g, dev, sizeof(T), batch, threads, smem, staged, grid)) != \
             cudaSuccess)                                                                                   \
@@ -715,9 +721,14 @@ cudaError_t launch_shuffle_product(const Geometry& g, const DeviceInfo& dev, cud
         kernel<<<grid, threads, smem, s>>>(g, static_cast<int>(kind), out, add, lhs, rhs, batch,           \
                                            static_cast<T>(alpha), static_cast<T>(beta), staged, ord);      \
     }
-    if (g.depth <= 8) RPP_GB_SHUFFLE_FWD(8)
-    else if (g.depth <= 16) RPP_GB_SHUFFLE_FWD(16)
-    else RPP_GB_SHUFFLE_FWD(32)
+    const bool scale = static_cast<T>(beta) != T(1);
+    if (g.depth <= 8) {
+        if (scale) RPP_GB_SHUFFLE_FWD(8, true) else RPP_GB_SHUFFLE_FWD(8, false)
+    } else if (g.depth <= 16) {
+        if (scale) RPP_GB_SHUFFLE_FWD(16, true) else RPP_GB_SHUFFLE_FWD(16, false)
+    } else {
+        if (scale) RPP_GB_SHUFFLE_FWD(32, true) else RPP_GB_SHUFFLE_FWD(32, false)
+    }
 #undef RPP_GB_SHUFFLE_FWD
     return cudaGetLastError();
 }
@@ -726,19 +737,26 @@ template <typename T>
 cudaError_t launch_shuffle_adjoint(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, ShuffleAdjKind kind,
                                    TArg<T> out, TArg<T> op, TArg<T> arg, int64_t batch, double beta) {
     if (batch <= 0) return cudaSuccess;
-    constexpr auto kernel = k_shuffle_adjoint<T>;
-    cudaError_t err = allow_large_smem<kernel>(dev);
-    if (err != cudaSuccess) return err;
-    int threads, staged;
-    size_t smem;
-    dim3 grid;
-    if ((err = shuffle_launch_shape(kernel, g, dev, sizeof(T), batch, threads, smem, staged, grid)) != cudaSuccess)
-        return err;
-    const ShuffleOrder ord = shuffle_adjoint_order(g, kind, out.lo, out.hi, op.lo, op.hi, arg.lo, arg.hi, threads);
-    if (ord.start[ord.count] == 0) return cudaSuccess;
-    kernel<<<grid, threads, smem, s>>>(g, static_cast<int>(kind), out, op, arg, batch, static_cast<T>(beta), staged,
-                                       ord);
-    return cudaGetLastError();
+    auto run = [&](auto kernel_c) -> cudaError_t {
+        constexpr auto kernel = decltype(kernel_c)::value;
+        cudaError_t err = allow_large_smem<kernel>(dev);
+        if (err != cudaSuccess) return err;
+        int threads, staged;
+        size_t smem;
+        dim3 grid;
+        if ((err = shuffle_launch_shape(kernel, g, dev, sizeof(T), batch, threads, smem, staged, grid)) !=
+            cudaSuccess)
+            return err;
+        const ShuffleOrder ord =
+            shuffle_adjoint_order(g, kind, out.lo, out.hi, op.lo, op.hi, arg.lo, arg.hi, threads);
+        if (ord.start[ord.count] == 0) return cudaSuccess;
+        kernel<<<grid, threads, smem, s>>>(g, static_cast<int>(kind), out, op, arg, batch, static_cast<T>(beta),
+                                           staged, ord);
+        return cudaGetLastError();
+    };
+    if (static_cast<T>(beta) == T(1))
+        return run(std::integral_constant<decltype(&k_shuffle_adjoint<T, false>), &k_shuffle_adjoint<T, false>>{});
+    return run(std::integral_constant<decltype(&k_shuffle_adjoint<T, true>), &k_shuffle_adjoint<T, true>>{});
 }
 
 template <typename T>
