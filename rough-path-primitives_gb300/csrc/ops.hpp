@@ -106,6 +106,7 @@ enum class ShuffleAdjKind : int {
 struct ShuffleOrder {
     int count;
     int warp_entries;
+    int tasked;  // adjoints: entries [tasked, count) have no terms and are zero-filled, not queued
     int deg[kMaxDepth + 1];
     uint32_t start[kMaxDepth + 2];
 };

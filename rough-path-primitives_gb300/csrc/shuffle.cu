@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind
     __shared__ uint32_t s_next;
     const int ohi = imin(op.hi, G.depth), ahi = imin(arg.hi, G.depth);
     const uint32_t nwarp = ord.start[ord.warp_entries];
-    const uint32_t total = ord.start[ord.count];
+    const uint32_t total = ord.start[ord.tasked];
     const uint32_t ntasks = nwarp + (total - nwarp + 31) / 32;
     const int lane = threadIdx.x & 31;
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
@@ -570,6 +570,15 @@ __global__ void __launch_bounds__(256, 3) k_shuffle_adjoint(Geometry G, int kind
             if (!st.commit(G.fault)) return;
         } else {
             __syncthreads();
+        }
+        // degrees without terms (e.g. the top degree of the left adjoint):
+        // coalesced zero stores by the whole CTA instead of one queued task
+        // per 32 coefficients (after the inputs are read or staged, as every
+        // other write)
+        for (int i = ord.tasked; i < ord.count; ++i) {
+            T* z = o + G.db[ord.deg[i]];
+            const uint32_t len = G.pw[ord.deg[i]];
+            for (uint32_t u = threadIdx.x; u < len; u += blockDim.x) z[u] = T(0);
         }
         for (;;) {
             uint32_t t = 0;
@@ -645,6 +654,7 @@ ShuffleOrder shuffle_product_order(const Geometry& g, int out_lo, int out_hi) {
         ++o.count;
     }
     o.start[o.count] = acc;
+    o.tasked = o.count;
     return o;
 }
 
@@ -698,6 +708,8 @@ ShuffleOrder shuffle_adjoint_order(const Geometry& g, ShuffleAdjKind kind, int o
     }
     o.count = count;
     o.start[count] = acc;
+    o.tasked = count;
+    while (o.tasked > o.warp_entries && e[o.tasked - 1].cost == 0.0) --o.tasked;
     return o;
 }
 
