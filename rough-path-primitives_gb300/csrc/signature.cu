@@ -150,8 +150,9 @@ constexpr uint32_t kRowMin = 32;
 // reverse step ends with a butterfly of about 2 WT adds, against log2(32/W)
 // for the letter-specialised loop.  Measured against that loop on fused
 // forward + reverse launches: W2 D12 +12.8 %, W3 D8 +7.1 %, W6 D6 +5.8 %,
-// W4 D6 and W7 D4 equal, W5 D5 -7 % and W8 D4 -7.5 % (the butterfly's adds are
-// 4-6 % of a thread's FMAs per step there).
+// W4 D6 equal, W5 D5 -7 % and W8 D4 -7.5 % (the butterfly's adds are 4-6 % of
+// a thread's FMAs per step there).  Widths without an instantiation (WT = 0)
+// keep the generic loop.
 template <int WT>
 constexpr bool kFusedLetters = kRowModeB<WT> && (WT == 2 || WT == 3 || WT == 6);
 
