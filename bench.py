@@ -12,8 +12,11 @@ explicit L2 flush is needed between steps.
 Prints one JSON line (rank 0).  `value` times the kernel with inputs resident
 in HBM; `e2e` times the same through the public API with pinned host buffers
 (H2D of increments + seeds, D2H of signatures + gradients inside the timed
-region).  `--impl reference` times the CPU oracle (the reference algorithm
-restated in C) on the host cores for a bounded sample of the same workload.
+region).  `--impl reference` times the reference's CPU implementation of the
+same computation on the host cores (the reference's own CPU strategy, compiled
+from its headers into oracle/_ref where they were installed; else the oracle's
+C restatement) for a bounded sample of the same workload.  `--gpus N` without
+torch.distributed's environment relaunches itself with one process per GPU.
 """
 from __future__ import annotations
 
@@ -111,29 +114,46 @@ def make_inputs(seed: int, batch: int):
     return incr, ell
 
 
+def headline_config(batch: int, world: int) -> dict:
+    """The workload's description, shared by both arms' JSON lines."""
+    return {"workload": "signature_fwd_bwd_w5_d5_l256", "width": WIDTH, "depth": DEPTH, "batch_per_gpu": batch,
+            "length": LENGTH, "increments": "N(0,1/256) iid", "seed_functional": "U[-1,1]",
+            "l2": "inputs+outputs 340 MB > L2 (no flush needed)", "parallelism": f"replicas x{world}"}
+
+
 def cpu_reference(steps: int, warmup: int, world: int, rank: int):
-    """CPU arm: the oracle's signature forward + stored-prefix reverse pass on
-    all host cores, each step a bounded sample of the workload's paths."""
+    """CPU arm: the signature forward pass and the stored-prefix reverse pass
+    on all host cores, each step a bounded sample of the workload's paths.
+    Runs the reference itself (its CPU strategy compiled from its headers into
+    oracle/_ref by build(), driven through its public operations) where that
+    library was built, else the oracle's C restatement of the same algorithm."""
     if rank != 0:
         return None
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    orc = O.Oracle()
+    if os.path.exists(O.REF_LIB_PATH):
+        impl, kind = O.RefBridge(), "reference"
+        what = ("the reference's SingleThreadStrategy<double> through rpp::ops: ft_fmexp forward storing "
+                "prefixes, then ft_exp, ft_adj_lmul, ft_adj_rmul per increment")
+    else:
+        impl, kind = O.Oracle(), "port"
+        what = "the oracle's C restatement of the reference's forward and stored-prefix reverse pass"
     cores = os.cpu_count() or 1
     sample = max(cores, 2 * cores)
     incr, ell = make_inputs(1234, sample)
     offs = np.arange(sample + 1, dtype=np.int64) * LENGTH
     for _ in range(max(0, warmup)):
-        orc.signature(WIDTH, DEPTH, incr, offs, ell=ell, threads=cores)
+        impl.signature(WIDTH, DEPTH, incr, offs, ell=ell, threads=cores)
     times = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        orc.signature(WIDTH, DEPTH, incr, offs, ell=ell, threads=cores)
+        impl.signature(WIDTH, DEPTH, incr, offs, ell=ell, threads=cores)
         times.append(time.perf_counter() - t0)
     total = sum(times)
-    return {"value": sample * steps / total, "unit": "paths/s", "cores": cores, "kind": "port",
-            "sample": f"{sample} of the {BATCH} paths per step (W5 D5 L256 FP64 forward + stored-prefix reverse)",
+    return {"value": sample * steps / total, "unit": "paths/s", "cores": cores, "kind": kind,
+            "sample": f"{sample} of the {BATCH} paths per step (W5 D5 L256 FP64, forward + stored-prefix "
+                      f"reverse; {what}; {cores} threads)",
             "ms_per_step": 1e3 * total / steps}
 
 
@@ -535,8 +555,7 @@ def run_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "paths/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "signature_fwd_bwd_w5_d5_l256", "width": WIDTH, "depth": DEPTH, "batch": BATCH,
-                   "length": LENGTH, "sample_paths_per_step": base["sample"]},
+        "config": headline_config(args.batch, world),
         "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": base["value"], "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -560,6 +579,16 @@ def main():
                     help="other configurations instead of the headline: ft_mul, logsig, ragged, w6d6, w2d12, "
                          "w16d3, adjoints, shuffle, lie_exp or all (comma-separated)")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch this command under torch.distributed.run
+        import socket
+
+        with socket.socket() as sock:
+            sock.bind(("127.0.0.1", 0))
+            port = sock.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+        raise SystemExit(subprocess.call(cmd))
     if args.impl == "reference":
         run_reference_arm(args)
         return
@@ -742,19 +771,16 @@ def main():
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "signature_fwd_bwd_w5_d5_l256", "width": WIDTH, "depth": DEPTH,
-                   "batch_per_gpu": batch, "length": LENGTH, "increments": "N(0,1/256) iid",
-                   "seed_functional": "U[-1,1]", "l2": "inputs+outputs 340 MB > L2 (no flush needed)",
-                   "kernel": ("fused forward+reverse: a forward launch and a reverse launch per step"
-                              if tuned_threads & (1 << 14) else "fused forward+reverse, one launch per step"),
-                   "parallelism": f"replicas x{world}",
-                   "schedule": {"threads_per_cta": tuned_threads & 1023,
-                                "ctas_per_sm_cap": (tuned_threads >> 10) & 15,
-                                "two_launches": bool(tuned_threads & (1 << 14)),
-                                "forward_top_level_in_global": bool(tuned_threads & (1 << 15)),
-                                "reverse_threads_per_cta": ((tuned_threads >> 16) & 1023) or (tuned_threads & 1023),
-                                "cotangent_in_global": bool(tuned_threads & (1 << 26)),
-                                "chosen_by": "rpp_gb_signature_tune" if pinned is None else "--schedule"}},
+        "config": headline_config(batch, world),
+        "kernel": ("fused forward+reverse: a forward launch and a reverse launch per step"
+                   if tuned_threads & (1 << 14) else "fused forward+reverse, one launch per step"),
+        "schedule": {"threads_per_cta": tuned_threads & 1023,
+                     "ctas_per_sm_cap": (tuned_threads >> 10) & 15,
+                     "two_launches": bool(tuned_threads & (1 << 14)),
+                     "forward_top_level_in_global": bool(tuned_threads & (1 << 15)),
+                     "reverse_threads_per_cta": ((tuned_threads >> 16) & 1023) or (tuned_threads & 1023),
+                     "cotangent_in_global": bool(tuned_threads & (1 << 26)),
+                     "chosen_by": "rpp_gb_signature_tune" if pinned is None else "--schedule"},
         "roofline": {"bound": "fp64_fma", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": (achieved / fp64_peak) if fp64_peak else None,
                      "traffic": TWO_LAUNCH_TRAFFIC_BYTES if tuned_threads & (1 << 14) else None,

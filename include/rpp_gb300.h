@@ -397,8 +397,14 @@ int rpp_gb_signature_host(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t
  * depth 6 in FP64).  All calls share the array and it keeps the previous
  * call's contents (each call re-initialises what it reads), so calls whose
  * launches may overlap on the GPU race and must be serialised by the caller.
+ * A schedule recorded by rpp_gb_signature_tune for the same shape is used,
+ * except that a launch it gives a cotangent workspace (bit 26, an
+ * allocation) keeps its cotangent arrays in shared memory instead; a schedule
+ * whose launch would need a workspace is refused before anything is launched.
  * The first call on each device looks up the array's device address (with
- * that device current); make that first call before any stream capture. */
+ * that device current) and keeps it for the life of the process, which
+ * assumes the device's context is not destroyed while the library is in use;
+ * make that first call before any stream capture. */
 int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
                                     const void* incr, const int64_t* offsets, int64_t length,
                                     int64_t batch, void* sig, int64_t sig_stride, const void* seed,

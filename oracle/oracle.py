@@ -440,6 +440,7 @@ class RefBridge(Oracle):
         L.ref_conversion_matrix.restype = i64
         L.ref_tensor_lie.argtypes = [i32, i32, i64, ctypes.c_int, i64, i64, i64, vp, vp, vp, vp, i64, vp, i64]
         L.ref_signature.argtypes = [i32, i32, i64, vp, vp, vp, i32]
+        L.ref_signature_grad.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, i32]
         L.ref_st.argtypes = [i32, i32, i64, ctypes.c_int, P, P, P, P, dbl, dbl]
         L.ref_st_adj_mul.argtypes = [i32, i32, i64, P, P, P]
         L.ref_left_hs_mul.argtypes = [i32, i32, i64, P, P, P, dbl]
@@ -529,13 +530,22 @@ class RefBridge(Oracle):
                                           arg.ctypes.data, arg.shape[1]))
 
     def signature(self, W, D, incr, offsets, ell=None, want_sig=True, threads=1):
-        assert ell is None, "the reference has no reverse-mode signature"
+        """Forward: the caller loop of ft_fmexp.  With ell, also the gradient of
+        sum_b <ell_b, S(x_b)> by the stored-prefix reverse pass composed from
+        the reference's ft_exp, ft_adj_lmul and ft_adj_rmul."""
         incr = np.ascontiguousarray(incr, dtype=np.float64)
         offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         B = len(offsets) - 1
-        sig = np.zeros((B, tensor_dim(W, D)))
-        self._chk(self.lib.ref_signature(W, D, B, incr.ctypes.data, offsets.ctypes.data, sig.ctypes.data, threads))
-        return sig, None
+        sig = np.zeros((B, tensor_dim(W, D))) if want_sig or ell is None else None
+        if ell is None:
+            self._chk(self.lib.ref_signature(W, D, B, incr.ctypes.data, offsets.ctypes.data, sig.ctypes.data,
+                                             threads))
+            return sig, None
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        grad = np.zeros_like(incr)
+        self._chk(self.lib.ref_signature_grad(W, D, B, incr.ctypes.data, offsets.ctypes.data, ell.ctypes.data,
+                                              None if sig is None else sig.ctypes.data, grad.ctypes.data, threads))
+        return sig, grad
 
     def _st(self, W, D, mode, out, a, b, c, ranges, alpha, beta):
         n, s = out.shape

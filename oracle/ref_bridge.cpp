@@ -261,6 +261,116 @@ int ref_signature(int32_t W, int32_t D, int64_t n, double const* incr, int64_t c
     return 0;
 }
 
+// Forward signature and the stored-prefix reverse pass of a ragged batch,
+// each path by the reference's own operations (the CPU form of the
+// per-operation composition a reference user writes for the gradient of
+// loss = sum_b <ell_b, S(x_b)>):
+//   forward   S_k = ft_fmexp(S_{k-1}, X_k), every prefix stored;
+//   reverse   G_L = ell_b; for k = L..1:
+//               E   = ft_exp(X_k)
+//               H   = ft_adj_lmul(S_{k-1}, G_k)       (d loss / d E_k)
+//               grad x_k = H contracted with dE_k/dx_k  (no reference op: the
+//                          derivative of prod_i x[w_i] / |w|! in each letter)
+//               G_{k-1} = ft_adj_rmul(E, G_k).
+// X_k holds increment k in degree one.  `sig` (may be null) receives S_L.
+// Paths are split over `threads` host threads, each issuing its own calls.
+int ref_signature_grad(int32_t W, int32_t D, int64_t n, double const* incr, int64_t const* offsets,
+                       double const* ell, double* sig, double* grad, int32_t threads) {
+    BasisData bd(W, D);
+    const Index dim = bd.basis.size();
+    if (threads < 1) threads = 1;
+    std::vector<int> rc(static_cast<size_t>(threads), 0);
+    auto full = [&](double* p) { return rpp::make_tensor_batch(p, dim, Degree{0}, Degree{D}); };
+    auto cfull = [&](double const* p) { return rpp::make_tensor_batch(p, dim, Degree{0}, Degree{D}); };
+    auto work = [&](int t, int64_t b0, int64_t b1) {
+        std::vector<double> G(static_cast<size_t>(dim)), Gn(static_cast<size_t>(dim)), H(static_cast<size_t>(dim)),
+            E(static_cast<size_t>(dim)), x(static_cast<size_t>(1 + W), 0.0), before(static_cast<size_t>(D) + 1),
+            after(static_cast<size_t>(D) + 1);
+        std::vector<int> letters(static_cast<size_t>(D) + 1);
+        std::vector<double> prefixes;
+        auto fail = [&](auto const& err) {
+            rc[static_cast<size_t>(t)] = 1 + static_cast<int>(err.code());
+        };
+        for (int64_t b = b0; b < b1; ++b) {
+            const int64_t off = offsets[b], len = offsets[b + 1] - off;
+            prefixes.assign(static_cast<size_t>(dim * (len + 1)), 0.0);
+            prefixes[0] = 1.0;
+            for (int64_t k = 0; k < len; ++k) {
+                std::memcpy(x.data() + 1, incr + (off + k) * W, sizeof(double) * static_cast<size_t>(W));
+                auto xb = rpp::make_tensor_batch(static_cast<double const*>(x.data()), static_cast<Index>(1 + W),
+                                                 Degree{1}, Degree{1});
+                if (auto err = rpp::ops::ft_fmexp(Strategy{}, {}, full(prefixes.data() + (k + 1) * dim),
+                                                  cfull(prefixes.data() + k * dim), xb, bd.basis, 1);
+                    !err) {
+                    fail(err);
+                    return;
+                }
+            }
+            if (sig) std::memcpy(sig + b * dim, prefixes.data() + len * dim, sizeof(double) * static_cast<size_t>(dim));
+            if (!grad) continue;
+            std::memcpy(G.data(), ell + b * dim, sizeof(double) * static_cast<size_t>(dim));
+            for (int64_t k = len - 1; k >= 0; --k) {
+                double const* xk = incr + (off + k) * W;
+                std::memcpy(x.data() + 1, xk, sizeof(double) * static_cast<size_t>(W));
+                auto xb = rpp::make_tensor_batch(static_cast<double const*>(x.data()), static_cast<Index>(1 + W),
+                                                 Degree{1}, Degree{1});
+                if (auto err = rpp::ops::ft_exp(Strategy{}, {}, full(E.data()), xb, bd.basis, 1); !err) {
+                    fail(err);
+                    return;
+                }
+                if (auto err = rpp::ops::ft_adj_lmul(Strategy{}, {}, full(H.data()), cfull(prefixes.data() + k * dim),
+                                                     cfull(G.data()), bd.basis, 1);
+                    !err) {
+                    fail(err);
+                    return;
+                }
+                double* g = grad + (off + k) * W;
+                for (int32_t a = 0; a < W; ++a) g[a] = 0.0;
+                double fact = 1.0;
+                Index begin = 1, width_n = 1;
+                for (int32_t deg = 1; deg <= D; ++deg) {
+                    fact *= deg;
+                    width_n *= W;
+                    for (Index i = 0; i < width_n; ++i) {
+                        const double h = H[static_cast<size_t>(begin + i)];
+                        if (h == 0.0) continue;
+                        Index r = i;
+                        for (int32_t p = deg - 1; p >= 0; --p) {
+                            letters[static_cast<size_t>(p)] = static_cast<int>(r % W);
+                            r /= W;
+                        }
+                        before[0] = 1.0;
+                        for (int32_t p = 0; p < deg; ++p) before[p + 1] = before[p] * xk[letters[p]];
+                        after[deg] = 1.0;
+                        for (int32_t p = deg - 1; p >= 0; --p) after[p] = after[p + 1] * xk[letters[p]];
+                        const double hs = h / fact;
+                        for (int32_t p = 0; p < deg; ++p) g[letters[p]] += hs * before[p] * after[p + 1];
+                    }
+                    begin += width_n;
+                }
+                if (auto err = rpp::ops::ft_adj_rmul(Strategy{}, {}, full(Gn.data()), cfull(E.data()),
+                                                     cfull(G.data()), bd.basis, 1);
+                    !err) {
+                    fail(err);
+                    return;
+                }
+                G.swap(Gn);
+            }
+        }
+    };
+    const int64_t per = (n + threads - 1) / threads;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) {
+        const int64_t b0 = t * per, b1 = std::min<int64_t>(n, b0 + per);
+        if (b0 >= b1) break;
+        pool.emplace_back(work, t, b0, b1);
+    }
+    for (auto& th : pool) th.join();
+    for (int r : rc)
+        if (r) return r;
+    return 0;
+}
+
 // Shuffle algebra through the public front ends (include/rpp/operations/basic/
 // st_mul.hpp, st_fma.hpp, st_inplace_fma.hpp, st_adj_mul.hpp, left_hs_mul.hpp,
 // tensor_pairing.hpp).  mode 0: st_mul(out, b, c, beta); 1: st_fma(out, a, b,

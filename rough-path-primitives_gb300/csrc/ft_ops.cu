@@ -319,27 +319,30 @@ __global__ void k_helper(Geometry G, HelperKind kind, TArg<T> out, TArg<T> arg, 
 // E_n = E_{n-1} (x) x / n for a degree-one x, so the reverse of that Horner
 // recursion is, top level first,
 //     Ebar_{n-1}[u] += sum_a Ebar_n[ua] x_a / n,   dx_a += sum_u Ebar_n[ua] E_{n-1}[u] / n,
-// with Ebar = H initially.  One CTA per batch element; E and Ebar in shared
-// memory (2 * dim elements), one partial sum per thread for dx.
+// with Ebar = H initially.  One CTA per batch element; E and Ebar below the
+// top level in shared memory (2 * db[D] elements: the recursion never reads
+// E_D, and Ebar_D = H_D is only read, straight from global memory -- so the
+// widest states fit, 149 KB at W6 D6 FP64), one partial sum per thread for dx.
 template <typename T>
 __global__ void __launch_bounds__(256) k_exp_letter_vjp(Geometry G, const T* H, int64_t h_stride, const T* x,
                                                         int64_t x_stride, T* dx, int64_t dx_stride,
                                                         int64_t batch) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* E = reinterpret_cast<T*>(smem_raw);
-    T* Eb = E + G.dim;
-    T* part = Eb + G.dim;
-    const uint32_t W = static_cast<uint32_t>(G.width);
     const int D = G.depth;
+    const uint32_t lo = G.db[D];  // coefficients below the top level
+    T* E = reinterpret_cast<T*>(smem_raw);
+    T* Eb = E + lo;
+    T* part = Eb + lo;
+    const uint32_t W = static_cast<uint32_t>(G.width);
     const uint32_t slots = blockDim.x / W;
     const uint32_t my_a = threadIdx.x % W, my_slot = threadIdx.x / W;
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         const T* xb = x + b * x_stride;
         const T* hb = H + b * h_stride;
-        for (uint32_t i = threadIdx.x; i < G.dim; i += blockDim.x) Eb[i] = hb[i];
+        for (uint32_t i = threadIdx.x; i < lo; i += blockDim.x) Eb[i] = hb[i];
         if (threadIdx.x == 0) E[0] = T(1);
         __syncthreads();
-        for (int n = 1; n <= D; ++n) {
+        for (int n = 1; n < D; ++n) {
             const T inv = recip<T>().inv[n];
             for (uint32_t i = threadIdx.x; i < G.pw[n]; i += blockDim.x) {
                 uint32_t q, a;
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(256) k_exp_letter_vjp(Geometry G, const T* H, 
             const T inv = recip<T>().inv[n];
             const uint32_t wp = G.pw[n - 1];
             const T* En1 = E + G.db[n - 1];
-            const T* Ebn = Eb + G.db[n];
+            const T* Ebn = n == D ? hb + lo : Eb + G.db[n];
             T* Ebn1 = Eb + G.db[n - 1];
             for (uint32_t u = threadIdx.x; u < wp; u += blockDim.x) {
                 T s = T(0);
@@ -486,7 +489,7 @@ cudaError_t launch_exp_letter_vjp(const Geometry& g, const DeviceInfo& dev, cuda
     if (err != cudaSuccess) return err;
     const int threads = threads_for(g.pw[g.depth]);
     if (threads < g.width) return cudaErrorInvalidConfiguration;
-    const size_t smem = (2 * static_cast<size_t>(g.dim) + threads) * sizeof(T);
+    const size_t smem = (2 * static_cast<size_t>(g.db[g.depth]) + threads) * sizeof(T);
     if (smem > static_cast<size_t>(dev.max_smem_optin)) return cudaErrorInvalidConfiguration;
     dim3 grid;
     if ((err = batch_grid(kernel, dev, threads, smem, batch, grid)) != cudaSuccess) return err;

@@ -179,6 +179,9 @@ constexpr int kScheduleReverseShift = 16;
 // the forward chains in shared memory and the cotangent level and chains in
 // a per-CTA global workspace (L2-resident), so more CTAs fit per SM.
 constexpr int kScheduleCotangentGlobal = 1 << 26;
+// kScheduleMergedReverse: reverse steps with D barriers (the recovery of the
+// prefix beside the transposition of the cotangent chains) instead of 2D - 1.
+constexpr int kScheduleMergedReverse = 1 << 27;
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,

@@ -62,7 +62,17 @@ struct SigGeometry {
 // less than one level (W2 D12 FP64: 229 KB, 196 KB without its top) still
 // runs resident.  Level D is only ever updated by the thread that owns the
 // coefficient, so no barrier orders these accesses.
-enum SigMode : int { kForward = 1, kBackward = 2, kLoadFinal = 4, kTopLevel = 8, kTopGlobal = 16, kCotGlobal = 32 };
+// kMergedReverse: reverse steps by backward_step_merged (D barriers) instead
+// of backward_step (2D - 1).
+enum SigMode : int {
+    kForward = 1,
+    kBackward = 2,
+    kLoadFinal = 4,
+    kTopLevel = 8,
+    kTopGlobal = 16,
+    kCotGlobal = 32,
+    kMergedReverse = 64
+};
 
 template <typename T>
 struct SigShared {
@@ -374,7 +384,7 @@ __device__ __forceinline__ void store_letter_partials(const SigShared<T>& sh, T 
 // other levels of G form one run of coefficients over all threads.
 template <typename T>
 __device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const SigShared<T>& sh, T* grad_k,
-                                                    bool update_g, uint32_t groups) {
+                                                    bool update_g, uint32_t groups, bool update_upper = true) {
     const Geometry& G = sg.g;
     const int D = G.depth;
     const uint32_t W = static_cast<uint32_t>(G.width);
@@ -396,7 +406,7 @@ __device__ __forceinline__ void finish_reverse_step(const SigGeometry& sg, const
             G1[a] = g;
         }
     }
-    if (update_g) {
+    if (update_g && update_upper) {
         uint32_t u = threadIdx.x;
         for (int i = 2; i < D; ++i) {
             const uint32_t wi = G.pw[i];
@@ -573,6 +583,155 @@ __device__ __forceinline__ void backward_step(const SigGeometry& sg, const SigSh
     __syncthreads();
 }
 
+// One reverse step with D barriers instead of 2D - 1.  The recovery of the
+// prefix (phase A, bottom-up) and the transposition of the cotangent chains
+// (phase B, top-down) touch disjoint arrays -- A reads and writes S and the
+// forward chains Tf, B reads G and the cotangent chains Tb and writes Tb --
+// so stage s (s = 1..D-1) runs A's level s beside B's level D+1-s.  Phase B's
+// letter gradients need every forward chain link, so they move to one last
+// stage, together with the update of G's levels 2..D-1; there each
+// coefficient (u, a) of a level is owned by one thread, which reads its old
+// G value (for the letter sum) before writing the updated one, so no barrier
+// separates the two.  G_1 and the gradient row are finished in the next
+// step's first stage by the gradient lanes, as in backward_step.  The sums are
+// the same as backward_step's in a different order.
+template <typename T, int WT>
+__device__ __forceinline__ void backward_step_merged(const SigGeometry& sg, const SigShared<T>& sh, const T* xc,
+                                                     T* xc_next, T x_next, T* pending_grad) {
+    const Geometry& G = sg.g;
+    const Width<WT> Wd(G);
+    const uint32_t W = Wd.value();
+    const int D = G.depth;
+    T* S = sh.S;
+    const T s0 = S[0];
+    const T* x1 = xc + W;
+    const uint32_t bd = blockDim.x;
+
+    // With D <= 2 stage 1's transposition overwrites Tb^D_1, which finishing
+    // the previous step reads: finish it in a stage of its own.
+    if (D <= 2 && pending_grad) {
+        finish_reverse_step(sg, sh, pending_grad, true, partial_groups(W), false);
+        __syncthreads();
+        pending_grad = nullptr;
+    }
+    for (int st = 1; st < D; ++st) {
+        if (st == 1 && pending_grad) finish_reverse_step(sg, sh, pending_grad, true, partial_groups(W), false);
+        uint32_t r = threadIdx.x;
+        // A: recover S_st of the prefix and the chain links T^n_st, n > st
+        {
+            const int j = st;
+            const uint32_t wj = G.pw[j];
+            T* Sj = S + G.db[j];
+            const T* own = chain(sg, sh.Tf, j, j - 1);
+            bool done = false;
+            if constexpr (kRowModeA<WT>) {
+                const uint32_t rows = G.pw[j - 1];
+                if (rows >= kRowMin) {
+                    for (; r < rows; r += bd) {
+                        const T o = own[r];
+                        T* Sq = Sj + r * WT;
+                        T sv[WT];
+#pragma unroll
+                        for (int a = 0; a < WT; ++a) {
+                            sv[a] = fma(-o, x1[a], Sq[a]);
+                            Sq[a] = sv[a];
+                        }
+                        for (int n = j + 1; n <= D; ++n) {
+                            const T p = chain(sg, sh.Tf, n, j - 1)[r];
+                            const T* xm = xc + (n - j + 1) * WT;
+                            T* dst = chain(sg, sh.Tf, n, j) + r * WT;
+#pragma unroll
+                            for (int a = 0; a < WT; ++a) dst[a] = fma(p, xm[a], sv[a]);
+                        }
+                    }
+                    r -= rows;
+                    done = true;
+                }
+            }
+            if (!done) {
+                for (; r < wj; r += bd) {
+                    uint32_t q, a;
+                    Wd.divmod(r, q, a);
+                    const T sv = fma(-(j == 1 ? s0 : own[q]), x1[a], Sj[r]);
+                    Sj[r] = sv;
+                    for (int n = j + 1; n <= D; ++n) {
+                        const T p = j == 1 ? s0 : chain(sg, sh.Tf, n, j - 1)[q];
+                        chain(sg, sh.Tf, n, j)[r] = fma(p, xc[(n - j + 1) * W + a], sv);
+                    }
+                }
+                r -= wj;
+            }
+        }
+        // B: the cotangent chains n = j..D from level j to level j - 1, j = D + 1 - st
+        {
+            const int j = D + 1 - st;
+            const uint32_t wjm1 = G.pw[j - 1];
+            for (int n = j; n <= D; ++n) {
+                if (r < wjm1) {
+                    const T* gin = n == j ? (j == D ? sh.top : sh.G + G.db[j]) : chain(sg, sh.Tb, n, j);
+                    T* gout = chain(sg, sh.Tb, n, j - 1);
+                    if constexpr (kRowModeB<WT>) {
+                        T x[WT];
+                        load_row(x, xc + (n - j + 2) * WT);
+                        for (; r < wjm1; r += bd) {
+                            const T* row = gin + r * WT;
+                            T acc = T(0);
+#pragma unroll
+                            for (int a = 0; a < WT; ++a) acc = fma(row[a], x[a], acc);
+                            gout[r] = acc;
+                        }
+                    } else {
+                        const T* xm = xc + (n - j + 2) * W;
+                        for (; r < wjm1; r += bd) {
+                            const T* row = gin + r * W;
+                            T acc = T(0);
+                            if constexpr (WT > 0) {
+#pragma unroll
+                                for (int a = 0; a < WT; ++a) acc = fma(row[a], xm[a], acc);
+                            } else {
+                                for (uint32_t a = 0; a < W; ++a) acc = fma(row[a], xm[a], acc);
+                            }
+                            gout[r] = acc;
+                        }
+                    }
+                }
+                r -= wjm1;
+            }
+        }
+        __syncthreads();
+    }
+
+    // Letter gradients of levels 2..D and the update of G_2..G_{D-1}.  Thread
+    // t takes letter t mod W of rows t / W, t / W + slots, ... (one run over
+    // the levels, offsets carried).
+    const uint32_t slots = bd / W;
+    const uint32_t my_a = threadIdx.x % W, my_slot = threadIdx.x / W;
+    T xacc = T(0);
+    if (my_slot < slots) {
+        uint32_t u = my_slot;
+        for (int j = 2; j <= D; ++j) {
+            const uint32_t rows = G.pw[j - 1];
+            T* Gj = j == D ? sh.top : sh.G + G.db[j];
+            for (; u < rows; u += slots) {
+                const uint32_t idx = u * W + my_a;
+                const T g = Gj[idx];
+                xacc = fma(g, chain(sg, sh.Tf, j, j - 1)[u], xacc);
+                T gn = g;
+                for (int n = j + 1; n <= D; ++n) {
+                    const T t = chain(sg, sh.Tb, n, j)[idx];
+                    xacc = fma(t, chain(sg, sh.Tf, n, j - 1)[u], xacc);
+                    gn = fma(sh.num[n - j + 1], t, gn);
+                }
+                if (j < D) Gj[idx] = gn;
+            }
+            u -= rows;
+        }
+    }
+    store_partials(sh, my_slot < slots ? xacc : T(0), W);
+    set_increment(sg, sh, xc_next, x_next);
+    __syncthreads();
+}
+
 // Kernel body.  With `gws` null every array lives in shared memory; otherwise
 // the state and chain arrays of CTA i live in gws + i*gws_stride (global
 // memory, L2-resident at the grid sizes used) and only the increments,
@@ -697,8 +856,12 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 512 ? (sizeof(T) == 4 ? 3 : 2) 
             for (int64_t k = len - 1; k >= 0; --k) {
                 const T x_next = xv;
                 if (k >= 2) xv = load_increment(sg, xin, k - 2);
-                backward_step<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k - 1), x_next,
-                                     k + 1 < len ? gout + (k + 1) * W : nullptr);
+                if (mode & kMergedReverse)
+                    backward_step_merged<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k - 1), x_next,
+                                                k + 1 < len ? gout + (k + 1) * W : nullptr);
+                else
+                    backward_step<T, WT>(sg, sh, xc_buf(sh, k), xc_buf(sh, k - 1), x_next,
+                                         k + 1 < len ? gout + (k + 1) * W : nullptr);
             }
             if (len > 0) {
                 finish_reverse_step(sg, sh, gout, false, partial_groups(W));
@@ -812,18 +975,25 @@ bool cap_residency(const DeviceInfo& dev, int threads, int cap, size_t& smem) {
     return true;
 }
 
-// `schedule` = CTA size in the low 10 bits (0: heuristic) and an optional cap
-// on CTAs per SM above them (0: as many as fit).
-template <typename T, int WT>
-cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStream_t s, const T* incr,
-                         PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride, T* grad,
-                         int mode, int schedule) {
+// How a launch runs: the shared-memory kernel (Resident), the same kernel
+// with its cotangent arrays in a stream-ordered global workspace
+// (CotangentWorkspace), or the global-workspace kernel for states larger than
+// one CTA's shared memory (Workspace).  Only Resident allocates nothing.
+enum class SigVariant { Invalid, Resident, CotangentWorkspace, Workspace };
+
+// The variant launch_width takes for `mode` under `schedule` (CTA size in the
+// low 10 bits, 0: heuristic; the cap bits are applied by the caller), with the
+// CTA size and dynamic shared memory of the shared-memory variants.  `mode`
+// may gain kTopGlobal (a state that misses shared memory by less than its top
+// level) and kCotGlobal.
+template <typename T>
+SigVariant choose_variant(const SigGeometry& sg, const DeviceInfo& dev, int& mode, int schedule, int& threads,
+                          size_t& smem) {
     const bool bwd = mode & kBackward;
     const int threads_req = schedule > 0 ? (schedule & 1023) : 0;
-    const int cap = schedule > 0 ? ((schedule >> 10) & 15) : 0;
-    int threads = threads_req > 0 ? threads_req : threads_for(sg.g.pw[sg.g.depth]);
-    if (threads % 32 != 0 || threads > kResidentMaxThreads) return cudaErrorInvalidConfiguration;
-    size_t smem = sig_smem_bytes<T>(sg, threads, bwd, true, mode & kTopGlobal);
+    threads = threads_req > 0 ? threads_req : threads_for(sg.g.pw[sg.g.depth]);
+    if (threads % 32 != 0 || threads > kResidentMaxThreads) return SigVariant::Invalid;
+    smem = sig_smem_bytes<T>(sg, threads, bwd, true, mode & kTopGlobal);
     // (the kernel also holds a few bytes of static shared memory)
     const size_t optin = static_cast<size_t>(dev.max_smem_optin);
     if (smem + 64 > optin && sig_smem_bytes<T>(sg, threads, bwd, true, true) + 64 <= optin) {
@@ -831,19 +1001,38 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
         smem = sig_smem_bytes<T>(sg, threads, bwd, true, true);
     }
     if (bwd && (schedule & kScheduleCotangentGlobal)) {
+        mode |= kCotGlobal;
+        smem = sig_smem_bytes<T>(sg, threads, false, true, mode & kTopGlobal);
+        if (smem + 64 > optin && !(mode & kTopGlobal)) {  // the top level to global memory too
+            mode |= kTopGlobal;
+            smem = sig_smem_bytes<T>(sg, threads, false, true, true);
+        }
+        return smem + 64 > optin ? SigVariant::Invalid : SigVariant::CotangentWorkspace;
+    }
+    return smem + 64 <= optin ? SigVariant::Resident : SigVariant::Workspace;
+}
+
+// `schedule` = CTA size in the low 10 bits (0: heuristic) and an optional cap
+// on CTAs per SM above them (0: as many as fit).
+template <typename T, int WT>
+cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStream_t s, const T* incr,
+                         PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride, T* grad,
+                         int mode, int schedule) {
+    const bool bwd = mode & kBackward;
+    const int cap = schedule > 0 ? ((schedule >> 10) & 15) : 0;
+    if (bwd && schedule > 0 && (schedule & kScheduleMergedReverse)) mode |= kMergedReverse;
+    int threads = 0;
+    size_t smem = 0;
+    const SigVariant variant = choose_variant<T>(sg, dev, mode, schedule, threads, smem);
+    if (variant == SigVariant::Invalid) return cudaErrorInvalidConfiguration;
+    if (variant == SigVariant::CotangentWorkspace) {
         // cotangent level and chains in a stream-ordered global workspace (one
         // slice per CTA, L2-resident: 30 MB for two CTAs per SM at W2 D12
         // FP64), state and forward chains resident: at W2 D12 FP64 the reverse
         // launch drops from 196 KB to 98 KB of shared memory per CTA, two CTAs
         // fit per SM, and fwd+bwd runs 49 079 -> 63 370 paths/s (with a
         // 512-thread reverse launch); at W5 D5 it is slower (105 748 -> 103 799)
-        mode |= kCotGlobal;
-        size_t hsmem = sig_smem_bytes<T>(sg, threads, false, true, mode & kTopGlobal);
-        if (hsmem + 64 > optin && !(mode & kTopGlobal)) {  // the top level to global memory too
-            mode |= kTopGlobal;
-            hsmem = sig_smem_bytes<T>(sg, threads, false, true, true);
-        }
-        if (hsmem + 64 > optin) return cudaErrorInvalidConfiguration;
+        const size_t hsmem = smem;
         constexpr auto kernel = k_signature<T, WT, kResidentMaxThreads, true>;
         cudaError_t err = allow_large_smem<kernel>(dev);
         if (err != cudaSuccess) return err;
@@ -859,7 +1048,7 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
         cudaError_t ferr = cudaFreeAsync(ws, s);
         return err != cudaSuccess ? err : ferr;
     }
-    if (smem + 64 <= optin) {
+    if (variant == SigVariant::Resident) {
         constexpr auto kernel = k_signature<T, WT, kResidentMaxThreads>;
         cudaError_t err = allow_large_smem<kernel>(dev);
         if (err != cudaSuccess) return err;
@@ -912,6 +1101,62 @@ cudaError_t launch_width_any(const SigGeometry& sg, const DeviceInfo& dev, cudaS
     }
 }
 
+// The launches of one call: one fused launch, or -- kScheduleSplit, a
+// forward+reverse call with signature output -- a forward launch and a
+// reverse launch from the final signatures; the reverse launch reads the
+// seed's top level from global memory, so both hold less shared memory per
+// CTA (more CTAs per SM) than the fused one.
+struct SigLaunches {
+    int count = 0;
+    int mode[2] = {0, 0};
+    int schedule[2] = {0, 0};
+};
+
+SigLaunches plan_launches(bool forward, bool has_sig, bool has_seed, bool has_grad, int threads) {
+    SigLaunches l;
+    const bool split = forward && has_sig && has_seed && has_grad && threads > 0 && (threads & kScheduleSplit);
+    if (split) {
+        const bool fwd_top_global = threads & kScheduleForwardTopGlobal;
+        const int rev = (threads >> kScheduleReverseShift) & 1023;
+        const int cot = threads & (kScheduleCotangentGlobal | kScheduleMergedReverse);
+        const int fwd = threads & ((1 << 14) - 1);  // CTA size and cap
+        l.count = 2;
+        l.mode[0] = kForward | kTopLevel | (fwd_top_global ? kTopGlobal : 0);
+        l.schedule[0] = fwd;
+        l.mode[1] = kBackward | kLoadFinal | kTopGlobal;
+        l.schedule[1] = (rev > 0 ? (fwd & ~1023) | rev : fwd) | cot;
+        return l;
+    }
+    int mode = 0;
+    if (forward) {
+        mode |= kForward;
+        if (has_seed && has_grad) mode |= kBackward;
+        // The top level of S is only an output: a gradient-only call skips it.
+        if (has_sig) mode |= kTopLevel;
+    } else {
+        mode |= kBackward | kLoadFinal;
+    }
+    l.count = 1;
+    l.mode[0] = mode;
+    l.schedule[0] = threads;
+    return l;
+}
+
+// Runs the launches; a ragged batch's work counter is re-armed between them.
+template <typename T>
+cudaError_t run_launches(const SigGeometry& sg, const DeviceInfo& dev, cudaStream_t s, const T* incr,
+                         PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride, T* grad,
+                         const SigLaunches& l) {
+    cudaError_t err = cudaSuccess;
+    for (int i = 0; i < l.count && err == cudaSuccess; ++i) {
+        if (i > 0 && paths.counter) err = cudaMemsetAsync(paths.counter, 0, sizeof(unsigned int), s);
+        if (err == cudaSuccess)
+            err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, l.mode[i],
+                                      l.schedule[i]);
+    }
+    return err;
+}
+
 }  // namespace
 
 template <typename T>
@@ -920,28 +1165,7 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
                              T* grad, bool forward, int threads) {
     if (paths.batch <= 0) return cudaSuccess;
     const SigGeometry sg = make_sig_geometry(g);
-    // Split schedule: a forward+reverse call with signature output runs as a
-    // forward launch and a reverse launch from the final signatures; the
-    // reverse launch reads the seed's top level from global memory, so both
-    // hold less shared memory per CTA (more CTAs per SM) than the fused one.
-    const bool split = forward && sig && seed && grad && threads > 0 && (threads & kScheduleSplit);
-    const bool fwd_top_global = split && (threads & kScheduleForwardTopGlobal);
-    int rev_threads = threads;
-    if (split) {
-        const int rev = (threads >> kScheduleReverseShift) & 1023;
-        const int cot = threads & kScheduleCotangentGlobal;
-        threads &= (1 << 14) - 1;  // CTA size and cap
-        rev_threads = (rev > 0 ? (threads & ~1023) | rev : threads) | cot;
-    }
-    int mode = 0;
-    if (forward) {
-        mode |= kForward;
-        if (seed && grad) mode |= kBackward;
-        // The top level of S is only an output: a gradient-only call skips it.
-        if (sig) mode |= kTopLevel;
-    } else {
-        mode |= kBackward | kLoadFinal;
-    }
+    const SigLaunches launches = plan_launches(forward, sig != nullptr, seed != nullptr, grad != nullptr, threads);
     // Ragged batches: order the paths longest first and hand them out through
     // a work counter (stream-ordered scratch, released after the launch).
     void* scratch = nullptr;
@@ -958,17 +1182,7 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
             return err;
         }
     }
-    cudaError_t err;
-    if (split) {
-        err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad,
-                                  kForward | kTopLevel | (fwd_top_global ? kTopGlobal : 0), threads);
-        if (err == cudaSuccess && paths.counter) err = cudaMemsetAsync(paths.counter, 0, sizeof(unsigned int), s);
-        if (err == cudaSuccess)
-            err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad,
-                                      kBackward | kLoadFinal | kTopGlobal, rev_threads);
-    } else {
-        err = launch_width_any<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-    }
+    cudaError_t err = run_launches<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, launches);
     if (scratch) {
         cudaError_t ferr = cudaFreeAsync(scratch, s);
         if (err == cudaSuccess) err = ferr;
@@ -994,7 +1208,9 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
 // holds a stand-in for the array's name; its device address is obtained once
 // per device, with that device current, by cudaGetSymbolAddress on the first
 // call made on that device (so that first call should come before any stream
-// capture).
+// capture) and kept for the life of the process: like the plans, whose device
+// tables live in the same context, it assumes the device's context is not
+// destroyed (cudaDeviceReset) while the library is in use.
 namespace {
 
 constexpr size_t kStaticScratchBytes = size_t(8) << 20;
@@ -1027,14 +1243,22 @@ cudaError_t launch_signature_static_scratch(const Geometry& g, const DeviceInfo&
     *refusal = StaticScratchRefusal::None;
     if (paths.batch <= 0) return cudaSuccess;
     const SigGeometry sg = make_sig_geometry(g);
-    int mode = kForward;
-    if (seed && grad) mode |= kBackward;
-    if (sig) mode |= kTopLevel;
-    // Only the shared-memory kernel: the global-workspace variant would need an allocation.
-    const int t = threads > 0 ? threads : threads_for(g.pw[g.depth]);
-    if (sig_smem_bytes<T>(sg, t, mode & kBackward, true, true) + 64 > static_cast<size_t>(dev.max_smem_optin)) {
-        *refusal = StaticScratchRefusal::StateTooLarge;
-        return cudaErrorNotSupported;
+    // A recorded schedule is honoured except for its cotangent workspace,
+    // which is an allocation: that launch runs with its cotangent arrays in
+    // shared memory instead (same results).
+    if (threads > 0) threads &= ~kScheduleCotangentGlobal;
+    const SigLaunches launches = plan_launches(true, sig != nullptr, seed != nullptr, grad != nullptr, threads);
+    // Only the shared-memory kernel allocates nothing: every launch of the
+    // call must take it, checked before anything is launched.
+    for (int i = 0; i < launches.count; ++i) {
+        int mode = launches.mode[i], t = 0;
+        size_t smem = 0;
+        const SigVariant v = choose_variant<T>(sg, dev, mode, launches.schedule[i], t, smem);
+        if (v == SigVariant::Workspace || v == SigVariant::CotangentWorkspace) {
+            *refusal = StaticScratchRefusal::StateTooLarge;
+            return cudaErrorNotSupported;
+        }
+        if (v == SigVariant::Invalid) return cudaErrorInvalidConfiguration;
     }
     if (paths.offsets && paths.batch > 1) {
         if (paths.batch > static_scratch_max_paths()) {
@@ -1046,20 +1270,13 @@ cudaError_t launch_signature_static_scratch(const Geometry& g, const DeviceInfo&
         if (err != cudaSuccess) return err;
         paths.counter = static_cast<unsigned int*>(base);
         paths.order = reinterpret_cast<int32_t*>(static_cast<char*>(base) + 256);
+        // rewrites the order and zeroes the counter: nothing of the previous
+        // call's contents is read
         k_order_by_length<<<1, 1024, 0, s>>>(paths.offsets, paths.batch, const_cast<int32_t*>(paths.order),
                                              paths.counter);
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
     }
-    switch (g.width) {
-        case 2: return launch_width<T, 2>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-        case 3: return launch_width<T, 3>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-        case 4: return launch_width<T, 4>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-        case 5: return launch_width<T, 5>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-        case 6: return launch_width<T, 6>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-        case 8: return launch_width<T, 8>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-        case 16: return launch_width<T, 16>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-        default: return launch_width<T, 0>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode, threads);
-    }
+    return run_launches<T>(sg, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, launches);
 }
 
 template cudaError_t launch_signature_static_scratch<float>(const Geometry&, const DeviceInfo&, cudaStream_t,

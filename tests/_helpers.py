@@ -16,6 +16,21 @@ def rel_err(actual, expected):
     return float(np.max(np.abs(actual - expected) / scale))
 
 
+def scaled_err(actual, expected):
+    """Error of a whole array against its own scale: max |a - e| / max(1,
+    max |e|).  The reference's metric (above) divides by each coefficient's own
+    magnitude with a floor of 1; a gradient coefficient is a sum of O(L) terms
+    of either sign and may cancel to near zero, so its error is measured
+    against the array's largest coefficient instead (equal to the reference's
+    metric wherever that coefficient is at most 1)."""
+    actual = np.asarray(actual, dtype=np.float64)
+    expected = np.asarray(expected, dtype=np.float64)
+    if actual.size == 0:
+        return 0.0
+    scale = max(1.0, float(np.max(np.abs(expected))))
+    return float(np.max(np.abs(actual - expected)) / scale)
+
+
 def assert_close(actual, expected, tol=TOL_F64, what=""):
     e = rel_err(actual, expected)
     assert np.isfinite(e) and e <= tol, f"{what}: relative error {e:.3e} > {tol:.1e}"

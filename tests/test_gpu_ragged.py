@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from _helpers import TOL_F32, TOL_F64, assert_close, rel_err
+from _helpers import TOL_F32, TOL_F64, assert_close, rel_err, scaled_err
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -22,7 +22,7 @@ def ragged(rng, n, lo, hi, W):
     return lengths, offsets, incr
 
 
-@pytest.mark.parametrize("dtype,tol", [(torch.float64, TOL_F64), (torch.float32, 10 * TOL_F32)])
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, TOL_F64), (torch.float32, TOL_F32)])
 def test_ragged_parity_against_oracle(orc, dtype, tol):
     W, D = 8, 4
     rng = np.random.default_rng(31)
@@ -43,15 +43,16 @@ def test_ragged_parity_against_oracle(orc, dtype, tol):
     esig, egrad = orc.signature(W, D, incr, offsets, ell=ell)
     assert_close(sig.double().cpu().numpy(), esig, tol, "ragged signature")
     g = grad.double().cpu().numpy()
-    scale = max(1.0, float(np.abs(egrad).max()))
-    assert rel_err(g / scale, egrad / scale) < tol * (1 if dtype == torch.float64 else 50)
+    e = scaled_err(g, egrad)
+    assert e <= tol, f"ragged gradient: scaled error {e:.3e}"
 
 
 def test_uneven_workload_in_cuda_graph(orc):
     """10,000 paths, lengths U{16..2048}, W8 D4, increments N(0, 1/len): one
     persistent launch per precision, both captured in one CUDA graph; replays
     equal the eager results bit for bit, FP64 matches the oracle on sampled
-    paths, FP32 is reported against FP64."""
+    paths, and FP32 is within 1e-5 of FP64 on every coefficient of every path
+    (the FP64 results being the oracle's to 1e-12, as the sampled paths show)."""
     W, D, B = 8, 4, 10_000
     rng = np.random.default_rng(2024)
     lengths, offsets, incr = ragged(rng, B, 16, 2048, W)
@@ -88,4 +89,4 @@ def test_uneven_workload_in_cuda_graph(orc):
         esig, _ = orc.signature(W, D, incr[offsets[b]:offsets[b + 1]], np.array([0, lengths[b]]))
         assert_close(s64[b].cpu().numpy()[None], esig, TOL_F64, f"path {b} (length {lengths[b]})")
     err32 = rel_err(s32.double().cpu().numpy(), s64.cpu().numpy())
-    assert err32 < 1e-4, err32
+    assert err32 <= TOL_F32, f"fp32 against fp64: relative error {err32:.3e}"

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from _helpers import assert_close
+from _helpers import TOL_F64, assert_close
 
 OPS_FILE = "ops_w3d4.npz"
 
@@ -153,3 +153,22 @@ def test_gradient_matches_finite_differences(orc):
             m[i, a] -= h
             fd[i, a] = ((orc.signature(W, D, p, offs)[0] - orc.signature(W, D, m, offs)[0]) * ell).sum() / (2 * h)
     assert np.max(np.abs(g - fd)) < 1e-7
+
+
+@pytest.mark.skipif(not os.path.exists(O.REF_LIB_PATH),
+                    reason="the reference's headers are not installed (oracle/_ref not built)")
+@pytest.mark.parametrize("W,D,lengths", [(3, 4, (5, 0, 17, 1)), (5, 5, (32, 9)), (2, 6, (11, 3, 7))])
+def test_reference_reverse_pass_matches_oracle(orc, W, D, lengths):
+    """The reference's own forward and stored-prefix reverse pass (its CPU
+    strategy driven through rpp::ops in oracle/_ref) against the oracle's
+    restatement, on ragged batches with empty and unit paths: the two CPU arms
+    the benchmark may time compute the same thing."""
+    ref = O.RefBridge()
+    rng = np.random.default_rng(W * 10 + D)
+    offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    incr = rng.normal(0, 0.3, (int(offsets[-1]), W))
+    ell = rng.uniform(-1, 1, (len(lengths), O.tensor_dim(W, D)))
+    rs, rg = ref.signature(W, D, incr, offsets, ell=ell, threads=2)
+    es, eg = orc.signature(W, D, incr, offsets, ell=ell)
+    assert_close(rs, es, TOL_F64, "reference signature")
+    assert_close(rg, eg, TOL_F64, "reference gradient")

@@ -1,14 +1,16 @@
 """The C++ drop-in (rpp/gpu/gb300/strategy.hpp) compiles against the
 reference's headers and turns the reference's own operation front ends into
 the right C-ABI calls.  Built with g++ against a recording test double of the
-C ABI, so no GPU is needed; skipped where the reference checkout is absent."""
+C ABI, so no GPU is needed; skipped where the reference's headers are absent
+(they are installed into baseline/_ref, or named by RPP_REFERENCE)."""
 import os
 import subprocess
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_INCLUDE = "/root/reference/include"
+REF_INCLUDE = os.path.join(os.environ.get("RPP_REFERENCE", os.path.join(ROOT, "baseline", "_ref")), "include")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 
 @pytest.fixture(scope="module")
@@ -17,12 +19,12 @@ def calls(tmp_path_factory):
         pytest.skip("reference headers not available")
     out = tmp_path_factory.mktemp("strategy") / "driver"
     cmd = ["g++", "-std=c++17", "-O0", "-I", REF_INCLUDE, "-I", os.path.join(ROOT, "include"),
-           "-I", os.path.join(ROOT, "rough-path-primitives_gb300", "include"), "-I", "/usr/local/cuda/include",
+           "-I", os.path.join(ROOT, "rough-path-primitives_gb300", "include"), "-I", os.path.join(CUDA_HOME, "include"),
            os.path.join(ROOT, "tests", "cpp", "strategy_driver.cpp"), os.path.join(ROOT, "tests", "cpp", "mock_capi.cpp"),
-           "-o", str(out), "-L/usr/local/cuda/lib64", "-lcudart"]
+           "-o", str(out), "-L" + os.path.join(CUDA_HOME, "lib64"), "-lcudart"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     res = subprocess.run([str(out)], capture_output=True, text=True,
-                         env={**os.environ, "LD_LIBRARY_PATH": "/usr/local/cuda/lib64"})
+                         env={**os.environ, "LD_LIBRARY_PATH": os.path.join(CUDA_HOME, "lib64")})
     assert res.returncode == 0, res.stdout + res.stderr
     return res.stdout.splitlines()
 
