@@ -185,6 +185,64 @@ def plain_path(pkg, strat, cfg, basis, incr, ell, batch, grad):
     return prefixes[L]
 
 
+REF_BLOCK_LIB = os.path.join(ROOT, "baseline", "_build", "libref_block.so")
+
+
+def _ref_block_lib():
+    """The reference's own GPU strategy (BlockStrategy<double, 128, 256>,
+    built by `make -C baseline` from the reference's headers), or None."""
+    import ctypes
+    if not os.path.exists(REF_BLOCK_LIB):
+        return None
+    lib = ctypes.CDLL(REF_BLOCK_LIB)
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+    lib.ref_block_tensor_set_identity.argtypes = [vp, i32, i32, vp, i64, i64]
+    lib.ref_block_ft_fmexp.argtypes = [vp, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32, i64]
+    lib.ref_block_ft_exp.argtypes = [vp, i32, i32, vp, i64, vp, i64, i32, i32, i64]
+    lib.ref_block_ft_adj_lmul.argtypes = [vp, i32, i32, vp, i64, vp, i64, vp, i64, i64]
+    lib.ref_block_ft_adj_rmul.argtypes = [vp, i32, i32, vp, i64, vp, i64, vp, i64, i64]
+    return lib
+
+
+def plain_reference_path(lib, pkg, strat, cfg, basis, xpad, incr, ell, batch, grad, stream):
+    """plain_path with the reference's own GPU kernels: the same loop (L
+    ft_fmexp launches storing every prefix, then per increment ft_exp,
+    ft_adj_lmul, the exp VJP and ft_adj_rmul), each operation run by the
+    reference's BlockStrategy except the exp VJP, which the reference does not
+    have (this repository's rpp_gb_exp_letter_vjp, about 2 dim FMAs per path
+    and step).  `xpad` holds the increments one element later than `incr`, so
+    that the degree-one view of increment k starts inside the allocation."""
+    import torch
+
+    W, D, L = WIDTH, DEPTH, LENGTH
+    dim = basis.size()
+    dev = incr.device
+    prefixes = torch.empty(L + 1, batch, dim, dtype=torch.float64, device=dev)
+    G, Gn, H, E = (torch.empty(batch, dim, dtype=torch.float64, device=dev) for _ in range(4))
+    s = stream.cuda_stream
+    xp = xpad.data_ptr()
+
+    def ok(rc, what):
+        if rc != 0:
+            raise RuntimeError(f"reference {what} failed with code {rc}")
+
+    ok(lib.ref_block_tensor_set_identity(s, W, D, prefixes[0].data_ptr(), dim, batch), "tensor_set_identity")
+    for k in range(L):
+        ok(lib.ref_block_ft_fmexp(s, W, D, prefixes[k + 1].data_ptr(), dim, prefixes[k].data_ptr(), dim,
+                                  xp + 8 * k * W, L * W, 1, 1, batch), "ft_fmexp")
+    G.copy_(ell)
+    for k in range(L - 1, -1, -1):
+        ok(lib.ref_block_ft_exp(s, W, D, E.data_ptr(), dim, xp + 8 * k * W, L * W, 1, 1, batch), "ft_exp")
+        ok(lib.ref_block_ft_adj_lmul(s, W, D, H.data_ptr(), dim, prefixes[k].data_ptr(), dim, G.data_ptr(), dim,
+                                     batch), "ft_adj_lmul")
+        pkg.exp_letter_vjp(strat, cfg, H, incr, grad, basis, batch, x_stride=L * W, dx_stride=L * W,
+                           x_offset=k * W, dx_offset=k * W).raise_if_failed()
+        ok(lib.ref_block_ft_adj_rmul(s, W, D, Gn.data_ptr(), dim, E.data_ptr(), dim, G.data_ptr(), dim, batch),
+           "ft_adj_rmul")
+        G, Gn = Gn, G
+    return prefixes[L]
+
+
 # ---------------------------------------------------------------------------
 # Other configurations (`--workload`), one JSON line each.  Device-resident
 # inputs; CUDA-event timing over `steps` launches after warm-up; FP64 peak
@@ -744,6 +802,36 @@ def main():
         del plain_grad, psig
         torch.cuda.empty_cache()
 
+    # the reference's own plain per-operation GPU path (its BlockStrategy) on
+    # the same inputs
+    plain_ref = None
+    ref_lib = None if args.no_plain else _ref_block_lib()
+    if ref_lib is not None:
+        ref_grad = torch.empty_like(incr)
+        xpad = torch.zeros(incr.numel() + 1, dtype=torch.float64, device=dev)
+        xpad[1:].copy_(incr.reshape(-1))
+        rsig = plain_reference_path(ref_lib, pkg, strat, cfg, basis, xpad, incr, ell, batch, ref_grad, stream)
+        torch.cuda.synchronize()
+        r_times = []
+        for _ in range(2):
+            e0.record(stream)
+            rsig = plain_reference_path(ref_lib, pkg, strat, cfg, basis, xpad, incr, ell, batch, ref_grad, stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            r_times.append(e0.elapsed_time(e1) / 1e3)
+        r_s = statistics.mean(r_times)
+        agree = float(torch.max(torch.abs(ref_grad - grad) / torch.clamp(torch.abs(grad), min=1.0)).item())
+        agree_sig = float(torch.max(torch.abs(rsig - sig) / torch.clamp(torch.abs(sig), min=1.0)).item())
+        plain_ref = {"value": batch / r_s, "unit": "paths/s", "ms_per_step": 1e3 * r_s,
+                     "launches_per_step": 1 + LENGTH + 4 * LENGTH,
+                     "kernels": "the reference's BlockStrategy<double, 128, 256> (its gpu/block operations, "
+                                "compiled from its headers for sm_103a): ft_fmexp x L (stored prefixes), then per "
+                                "increment ft_exp, ft_adj_lmul, ft_adj_rmul; the exp VJP (no reference "
+                                "operation) is this repository's kernel",
+                     "max_rel_diff_vs_fused": {"sig": agree_sig, "grad": agree}}
+        del ref_grad, rsig, xpad
+        torch.cuda.empty_cache()
+
     # parity spot check of this run's output against the oracle (3 paths)
     if rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -794,6 +882,8 @@ def main():
         "gpu_launches": args.steps * (2 if tuned_threads & (1 << 14) else 1),
         "plain": plain,
         "fused_over_plain": (value / world) / plain["value"] if plain else None,
+        "plain_reference": plain_ref,
+        "fused_over_plain_reference": (value / world) / plain_ref["value"] if plain_ref else None,
         "clocks": clk,
         "parity": {"max_rel_err_sig": s_err, "max_rel_err_grad": g_err, "paths_checked": 3},
     }
