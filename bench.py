@@ -418,9 +418,40 @@ def workload_lie_exp(pkg, torch, args, peak):
           extra={"composed_ms": ms_c, "fused_over_composed": ms_c / ms})
 
 
+def _graph_of(torch, fn):
+    """A CUDA graph of fn's launches (captured on a side stream)."""
+    stream = torch.cuda.Stream()
+    fn()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    stream.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            fn()
+    torch.cuda.current_stream().wait_stream(stream)
+    torch.cuda.synchronize()
+    return graph
+
+
+def _best_group(pkg, torch, candidates):
+    """The fastest (jobs, schedule) of a grouped launch, timed like the tuner
+    (CUDA events, a warm-up call first)."""
+    best = None
+    for jobs, sched in candidates:
+        if not pkg.signature_group(None, jobs, schedule=sched):
+            continue
+        ms = _time_launches(torch, lambda: pkg.signature_group(None, jobs, schedule=sched), 2, 1,
+                            torch.cuda.current_stream())
+        if best is None or ms < best[2]:
+            best = (jobs, sched, ms)
+    return best
+
+
 def workload_ragged(pkg, torch, args, peak):
-    """10,000 paths, lengths U{16..2048}, W8 D4, N(0, 1/len): one persistent
-    launch in FP64 and one in FP32, both replayed from one CUDA graph."""
+    """10,000 paths, lengths U{16..2048}, W8 D4, N(0, 1/len), run once in FP64
+    and once in FP32: ONE persistent launch for both precisions
+    (rpp_gb_signature_group) replayed from a CUDA graph; beside it the two
+    tuned separate launches replayed from one graph."""
     W, D, B = 8, 4, 10_000
     rng = np.random.default_rng(2024)
     lengths = rng.integers(16, 2049, B)
@@ -438,36 +469,144 @@ def workload_ragged(pkg, torch, args, peak):
     t32 = pkg.signature_tune(st32, None, x32, basis, B, offsets=off_d, out=s32)
     t64[0].raise_if_failed()
     t32[0].raise_if_failed()
-
-    def run():
-        pkg.signature(st64, None, x64, basis, B, offsets=off_d, out=s64)
-        pkg.signature(st32, None, x32, basis, B, offsets=off_d, out=s32)
-
-    stream = torch.cuda.Stream()
-    run()
-    torch.cuda.synchronize()
-    graph = torch.cuda.CUDAGraph()
-    stream.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(stream):
-        with torch.cuda.graph(graph, stream=stream):
-            run()
-    torch.cuda.current_stream().wait_stream(stream)
     cur = torch.cuda.current_stream()
-    ms = 1e3 * _time_launches(torch, graph.replay, args.steps, args.warmup, cur)
     ms64 = 1e3 * _time_launches(torch, lambda: pkg.signature(st64, None, x64, basis, B, offsets=off_d, out=s64),
                                 args.steps, args.warmup, cur)
     ms32 = 1e3 * _time_launches(torch, lambda: pkg.signature(st32, None, x32, basis, B, offsets=off_d, out=s32),
                                 args.steps, args.warmup, cur)
+    sep = _graph_of(torch, lambda: (pkg.signature(st64, None, x64, basis, B, offsets=off_d, out=s64),
+                                    pkg.signature(st32, None, x32, basis, B, offsets=off_d, out=s32)))
+    ms_sep = 1e3 * _time_launches(torch, sep.replay, args.steps, args.warmup, cur)
+    # the grouped launch: team sizes from the tuned separate launches, and a
+    # few alternatives; CTA sizes 640 / 512
+    cands = []
+    for th64, th32 in {(t64[1] & 1023, t32[1] & 1023), (128, 128), (128, 64), (256, 128), (128, 256),
+                       (256, 64)}:
+        jobs = [pkg.SignatureJob(st64, x64, basis, B, offsets=off_d, out=s64, threads=th64),
+                pkg.SignatureJob(st32, x32, basis, B, offsets=off_d, out=s32, threads=th32)]
+        for cta in (640, 512):
+            cands.append((jobs, cta))
+    jobs, sched, _ = _best_group(pkg, torch, cands)
+    graph = _graph_of(torch, lambda: pkg.signature_group(None, jobs, schedule=sched).raise_if_failed())
+    ms = 1e3 * _time_launches(torch, graph.replay, args.steps, args.warmup, cur)
+    # each job alone in the grouped kernel (its code and team layout against
+    # its own tuned launch)
+    alone = [1e3 * _time_launches(torch, lambda j=j: pkg.signature_group(None, [j], schedule=sched), args.steps,
+                                  args.warmup, cur) for j in jobs]
     err32 = float(torch.max(torch.abs(s32.double() - s64) / torch.clamp(s64.abs(), min=1.0)).item())
     steps_total = int(offsets[-1])
     flops64 = 2.0 * steps_total * step_fma(W, D)
-    _line("uneven-length signatures paths/sec (W8 D4, 10k paths, L~U[16,2048]), FP64 + FP32 in one graph",
+    _line("uneven-length signatures paths/sec (W8 D4, 10k paths, L~U[16,2048]), FP64 + FP32 in one launch",
           B / (ms / 1e3), "paths/s", ms, "f64+f32",
           {"workload": "ragged_w8_d4_b10000", "total_increments": steps_total,
-           "graph": "fp64 launch + fp32 launch", "schedule": {"f64": t64[1], "f32": t32[1]}},
-          extra={"fp64_ms": ms64, "fp32_ms": ms32, "fp64_paths_per_s": B / (ms64 / 1e3),
+           "graph": "one grouped launch (an FP64 job and an FP32 job)", "group_cta_threads": sched,
+           "group_team_threads": {"f64": jobs[0].arg.threads, "f32": jobs[1].arg.threads},
+           "schedule": {"f64": t64[1], "f32": t32[1]}},
+          extra={"gpu_launches": 2, "separate_launches_ms": ms_sep, "group_over_separate": ms_sep / ms,
+                 "group_fp64_job_alone_ms": alone[0], "group_fp32_job_alone_ms": alone[1],
+                 "fp64_ms": ms64, "fp32_ms": ms32, "fp64_paths_per_s": B / (ms64 / 1e3),
                  "fp32_paths_per_s": B / (ms32 / 1e3), "fp32_max_rel_err_vs_fp64": err32,
-                 "fp64_roofline_frac": flops64 / (ms64 / 1e3) / 1e12 / peak if peak else None})
+                 "fp64_roofline_frac": flops64 / (ms64 / 1e3) / 1e12 / peak if peak else None,
+                 "fp32_tflops": 2.0 * steps_total * step_fma(W, D) / (ms32 / 1e3) / 1e12})
+
+
+def workload_mixed(pkg, torch, args, peak):
+    """The large mixed-shape configuration: 16,384 paths of 64 increments
+    N(0, 1/64) at width 2 / depth 12 and 16,384 at width 16 / depth 3, FP64,
+    forward + reverse: ONE persistent launch for both shapes
+    (rpp_gb_signature_group) replayed from a CUDA graph, beside the two tuned
+    separate calls replayed from one graph."""
+    B, L = 16_384, 64
+    cur = torch.cuda.current_stream()
+    st = pkg.GB300Strategy(torch.float64)
+    parts, fma_total = [], 0
+    for W, D in ((2, 12), (16, 3)):
+        basis = pkg.TensorBasis(W, D)
+        dim = basis.size()
+        g = torch.Generator(device="cuda").manual_seed(W * 100 + D)
+        incr = torch.randn(B * L, W, dtype=torch.float64, device="cuda", generator=g) / np.sqrt(L)
+        ell = torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+        sig = torch.empty(B, dim, dtype=torch.float64, device="cuda")
+        grad = torch.empty_like(incr)
+        err, threads, _ = pkg.signature_tune(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad)
+        err.raise_if_failed()
+        parts.append((basis, incr, ell, sig, grad, threads))
+        fma_total += 4 * L * step_fma(W, D) * B
+
+    def separate():
+        for basis, incr, ell, sig, grad, _ in parts:
+            pkg.signature(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad).raise_if_failed()
+
+    sep = _graph_of(torch, separate)
+    ms_sep = 1e3 * _time_launches(torch, sep.replay, args.steps, args.warmup, cur)
+    cands = []
+    for t_deep in (256, 384, 512):
+        jobs = [pkg.SignatureJob(st, incr, basis, B, length=L, out=sig, seed=ell, grad=grad,
+                                 threads=t_deep if basis.width == 2 else 128)
+                for basis, incr, ell, sig, grad, _ in parts]
+        for sched in (640, 512, 640 | (1 << 27), 512 | (1 << 27)):
+            cands.append((jobs, sched))
+    jobs, sched, _ = _best_group(pkg, torch, cands)
+    graph = _graph_of(torch, lambda: pkg.signature_group(None, jobs, schedule=sched).raise_if_failed())
+    ms = 1e3 * _time_launches(torch, graph.replay, args.steps, args.warmup, cur)
+    alone = [1e3 * _time_launches(torch, lambda j=j: pkg.signature_group(None, [j], schedule=sched), args.steps,
+                                  args.warmup, cur) for j in jobs]
+    sep_alone = [1e3 * _time_launches(torch, lambda p=p: pkg.signature(st, None, p[1], p[0], B, length=L, out=p[3],
+                                                                       seed=p[2], grad=p[4]),
+                                      args.steps, args.warmup, cur) for p in parts]
+    _line("mixed-shape signature fwd+bwd paths/sec (W2 D12 + W16 D3, 2 x 16,384 paths, L64, FP64) in one launch",
+          2 * B / (ms / 1e3), "paths/s", ms, "f64",
+          {"workload": "mixed_w2d12_w16d3_b16384_l64", "group_schedule": sched,
+           "group_team_threads": [j.arg.threads for j in jobs], "separate_schedules": [p[5] for p in parts]},
+          flops=2.0 * fma_total, peak=peak,
+          extra={"gpu_launches": 2, "separate_launches_ms": ms_sep, "group_over_separate": ms_sep / ms,
+                 "group_job_alone_ms": {"w2d12": alone[0], "w16d3": alone[1]},
+                 "separate_alone_ms": {"w2d12": sep_alone[0], "w16d3": sep_alone[1]}})
+
+
+def workload_fp32(pkg, torch, args, peak):
+    """The headline shape in FP32: W5 D5, L256, 4096 paths, forward + reverse
+    (and forward only), against the FP32 FMA peak measured in the same run
+    (rpp_gb_fma_peak, FP32) and the FP64 oracle (1e-5)."""
+    import ctypes
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    W, D, B, L = WIDTH, DEPTH, BATCH, LENGTH
+    out = ctypes.c_double(0)
+    peak32 = out.value if pkg.library().rpp_gb_fma_peak(0, 0, ctypes.byref(out)) == 0 else None
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    st = pkg.GB300Strategy(torch.float32)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    incr64 = torch.randn(B * L, W, dtype=torch.float64, device="cuda", generator=g) / np.sqrt(L)
+    ell64 = torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    incr, ell = incr64.float(), ell64.float()
+    sig = torch.empty(B, dim, dtype=torch.float32, device="cuda")
+    grad = torch.empty_like(incr)
+    cur = torch.cuda.current_stream()
+    lines = []
+    for what, kw, fma in (("fwd+bwd", {"seed": ell, "grad": grad}, 4 * step_fma(W, D)),
+                          ("forward", {}, step_fma(W, D))):
+        err, threads, _ = pkg.signature_tune(st, None, incr, basis, B, length=L, out=sig, **kw)
+        err.raise_if_failed()
+        ms = 1e3 * _time_launches(torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, **kw),
+                                  args.steps, args.warmup, cur)
+        flops = 2.0 * fma * L * B
+        n = 3
+        esig, egrad = O.Oracle().signature(W, D, incr64[:n * L].cpu().numpy(), np.arange(n + 1) * L,
+                                           ell=ell64[:n].cpu().numpy() if kw else None)
+        err_sig = float(np.max(np.abs(sig[:n].double().cpu().numpy() - esig) / np.maximum(1, np.abs(esig))))
+        extra = {"fp32_tflops": flops / (ms / 1e3) / 1e12, "fp32_peak_tflops": peak32,
+                 "fp32_peak_frac": flops / (ms / 1e3) / 1e12 / peak32 if peak32 else None,
+                 "max_rel_err_sig_vs_fp64_oracle": err_sig}
+        if kw:
+            gg = grad[:n * L].double().cpu().numpy()
+            extra["max_scaled_err_grad_vs_fp64_oracle"] = float(np.max(np.abs(gg - egrad)) /
+                                                                max(1.0, float(np.max(np.abs(egrad)))))
+        _line(f"signature {what} paths/sec (W{W} D{D} L{L} FP32)", B / (ms / 1e3), "paths/s", ms, "f32",
+              {"workload": f"{what.replace('+', '_')}_w{W}_d{D}_l{L}_b{B}_fp32", "schedule": threads},
+              extra=extra)
 
 
 def workload_fwd_bwd(pkg, torch, args, peak, W, D, B, L, name):
@@ -488,8 +627,11 @@ def workload_fwd_bwd(pkg, torch, args, peak, W, D, B, L, name):
         torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad),
         args.steps, args.warmup, torch.cuda.current_stream())
     _line(f"signature fwd+bwd paths/sec (W{W} D{D} L{L} FP64)", B / (ms / 1e3), "paths/s", ms, "f64",
-          {"workload": name, "batch": B, "length": L, "threads_per_cta": threads & 1023,
-           "ctas_per_sm_cap": (threads >> 10) & 15, "two_launches": bool(threads & (1 << 14))},
+          {"workload": name, "batch": B, "length": L, "schedule": threads, "threads_per_cta": threads & 1023,
+           "ctas_per_sm_cap": (threads >> 10) & 15, "two_launches": bool(threads & (1 << 14)),
+           "top_level_in_global": bool(threads & (1 << 15)),
+           "cotangent_in_global": bool(threads & (1 << 26)), "d_barrier_reverse": bool(threads & (1 << 27)),
+           "cluster_ctas_per_path": ((threads >> 28) & 7) + 1},
           flops=2.0 * 4 * L * step_fma(W, D) * B, peak=peak)
 
 
@@ -579,7 +721,8 @@ def run_workloads(args):
     peak = _fp64_peak(pkg, 0)
     todo = args.workload.split(",")
     if "all" in todo:
-        todo = ["ft_mul", "logsig", "lie_exp", "ragged", "w6d6", "w2d12", "w16d3", "adjoints", "shuffle"]
+        todo = ["ft_mul", "logsig", "lie_exp", "ragged", "w6d6", "w2d12", "w16d3", "mixed", "fp32", "adjoints",
+                "shuffle"]
     for w in todo:
         if w == "ft_mul":
             workload_ft_mul(pkg, torch, args, peak)
@@ -593,6 +736,10 @@ def run_workloads(args):
             workload_fwd_bwd(pkg, torch, args, peak, 2, 12, 16384, 64, "fwd_bwd_w2_d12_l64_b16384")
         elif w == "w16d3":
             workload_fwd_bwd(pkg, torch, args, peak, 16, 3, 16384, 64, "fwd_bwd_w16_d3_l64_b16384")
+        elif w == "mixed":
+            workload_mixed(pkg, torch, args, peak)
+        elif w == "fp32":
+            workload_fp32(pkg, torch, args, peak)
         elif w == "lie_exp":
             workload_lie_exp(pkg, torch, args, peak)
         elif w == "shuffle":
@@ -635,7 +782,7 @@ def main():
                          "for profiling captures")
     ap.add_argument("--workload", default=None,
                     help="other configurations instead of the headline: ft_mul, logsig, ragged, w6d6, w2d12, "
-                         "w16d3, adjoints, shuffle, lie_exp or all (comma-separated)")
+                         "w16d3, mixed, fp32, adjoints, shuffle, lie_exp or all (comma-separated)")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # one process per GPU: relaunch this command under torch.distributed.run

@@ -428,8 +428,13 @@ int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream strea
  * (0: the same as the forward launch's), and bit 26 set when the launch with
  * the reverse pass keeps the cotangent arrays in a global workspace (the
  * state and forward chains stay in shared memory; more CTAs per SM for deep
- * narrow shapes).  A two-launch winner is refined by
- * timing other reverse sizes, then other forward sizes. */
+ * narrow shapes), bit 27 set for the reverse step with D barriers instead of
+ * 2D-1, and P-1 in bits 28-30 when each path's state is split over a
+ * thread-block cluster of P CTAs by first letter (P divides the width; one
+ * fused launch; bit 15 then puts the top level in the signature and seed
+ * rows) -- tried for states whose tensor exceeds 48 KB.  A two-launch winner
+ * is refined by timing other reverse sizes, then other forward sizes, and the
+ * three fastest schedules with a reverse pass are timed with bit 27 too. */
 int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
                           const void* incr, const int64_t* offsets, int64_t length, int64_t batch,
                           void* sig, int64_t sig_stride, const void* seed, int64_t seed_stride,
@@ -442,6 +447,44 @@ int rpp_gb_signature_with_schedule(const rpp_gb_plan* plan, rpp_gb_stream stream
                                    const void* incr, const int64_t* offsets, int64_t length,
                                    int64_t batch, void* sig, int64_t sig_stride, const void* seed,
                                    int64_t seed_stride, void* grad, int32_t schedule);
+
+/* Several signature calls in ONE persistent launch (no reference
+ * counterpart: the reference launches ft_fmexp once per increment and per
+ * shape).  Each job carries the arguments of one rpp_gb_signature call -- its
+ * plan (width, depth), dtype, equal-length or ragged increments, outputs --
+ * so one launch covers batches of different (width, depth) and of FP64 and
+ * FP32 together, e.g. inside one captured CUDA graph.  Each path of job j is
+ * run by a team of `threads` threads (a multiple of 32, at least
+ * width*depth; 0: the CTA size of the schedule recorded for that shape by
+ * rpp_gb_signature_tune, else a heuristic); a CTA holds as many teams of the
+ * job in progress as its threads and shared memory allow, so small states
+ * keep many paths per SM beside large ones.  CTAs take the jobs in order of
+ * their most expensive path and, inside a job, paths longest first from a
+ * work counter.  Each job's outputs equal, bit for bit, those of a separate
+ * rpp_gb_signature call with `threads` threads per CTA (and the same
+ * reverse-step form).  `schedule`: threads per CTA in bits 0-9 (at most 640;
+ * 0: 640) and bit 27 for the D-barrier reverse step.  Limits: 1 to 8 jobs,
+ * all plans on one device, each job's state in one team's shared memory
+ * (RPP_GB_NOT_IMPLEMENTED otherwise, e.g. width 6 depth 6 in FP64: run it
+ * with rpp_gb_signature), fewer than 2^31 paths per job.  Stream-ordered;
+ * the job order and work counters are allocated stream-ordered and released
+ * after the launch. */
+typedef struct rpp_gb_signature_job {
+    const rpp_gb_plan* plan;
+    int32_t dtype;
+    int32_t threads;
+    const void* incr;
+    const int64_t* offsets;
+    int64_t length;
+    int64_t batch;
+    void* sig;
+    int64_t sig_stride;
+    const void* seed;
+    int64_t seed_stride;
+    void* grad;
+} rpp_gb_signature_job;
+int rpp_gb_signature_group(rpp_gb_stream stream, const rpp_gb_signature_job* jobs, int32_t njobs,
+                           int32_t schedule);
 
 /* Vector-Jacobian product of exp for a degree-one argument (no reference
  * counterpart; it closes the stored-prefix reverse pass composed from

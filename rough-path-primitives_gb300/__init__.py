@@ -32,6 +32,7 @@ __all__ = [
     "tensor_generalised_antipode", "vector_assign", "vector_set_constant",
     "tensor_set_identity", "tensor_add_identity", "sparse_matrix_vector_product",
     "tensor_to_lie", "lie_to_tensor", "signature", "signature_backward", "signature_tune", "exp_letter_vjp",
+    "signature_host", "SignatureJob", "signature_group",
     "st_mul", "st_fma", "st_inplace_fma", "st_adj_mul", "left_hs_mul", "left_hs_adj_lmul", "left_hs_adj_rmul",
     "tensor_pairing", "make_scalar_batch", "tensor_log_to_lie", "lie_to_tensor_exp", "build", "library",
 ]
@@ -662,6 +663,40 @@ def signature(strategy, config, increments, basis, num_batches, *, length=None, 
     if schedule is not None:  # an explicit schedule (rpp_gb_signature_with_schedule)
         return _status(lib.rpp_gb_signature_with_schedule(*args, int(schedule)))
     return _status(lib.rpp_gb_signature(*args))
+
+
+class SignatureJob:
+    """One job of ``signature_group``: the arguments of one ``signature`` call
+    (its strategy -- hence dtype --, basis, increments with ``length`` or
+    ``offsets``, outputs) and ``threads``, the threads that run one of its
+    paths (0: the shape's tuned CTA size, else a heuristic)."""
+
+    def __init__(self, strategy, increments, basis, num_batches, *, length=None, offsets=None, out=None,
+                 out_stride=None, seed=None, seed_stride=None, grad=None, threads=0):
+        _check_batches(strategy, *(TensorBatch(t, 0, 0, 0) for t in (increments, out, seed, grad) if t is not None))
+        self.strategy, self.basis = strategy, basis
+        self.tensors = (increments, offsets, out, seed, grad)  # kept alive with the job
+        dim = basis.size()
+        self.arg = _lib.SignatureJobArg(
+            basis.plan(strategy.device), strategy.dtype_code(), int(threads), _ptr(increments), _ptr(offsets),
+            0 if length is None else int(length), num_batches, _ptr(out), dim if out_stride is None else out_stride,
+            _ptr(seed), dim if seed_stride is None else seed_stride, _ptr(grad))
+
+
+def signature_group(config, jobs, *, schedule=0) -> Error:
+    """Several ``signature`` calls -- different (width, depth) shapes and
+    precisions -- in one persistent launch (rpp_gb_signature_group).  ``jobs``:
+    a sequence of ``SignatureJob`` (1 to 8, one device).  Each job's outputs
+    equal those of its own ``signature`` call with ``schedule=job threads``.
+    ``schedule``: threads per CTA (bits 0-9, at most 640; 0: 640) and bit 27
+    for the D-barrier reverse step."""
+    jobs = list(jobs)
+    if not jobs:
+        raise ValueError("signature_group needs at least one job")
+    device = jobs[0].strategy.device
+    arr = (_lib.SignatureJobArg * len(jobs))(*(j.arg for j in jobs))
+    lib = _lib.load()
+    return _status(lib.rpp_gb_signature_group(_cfg(config).handle(device), arr, len(jobs), int(schedule)))
 
 
 def signature_host(strategy, config, increments, basis, num_batches, *, length, out=None, out_stride=None,

@@ -29,6 +29,25 @@ class TensorArg(ctypes.Structure):
     ]
 
 
+class SignatureJobArg(ctypes.Structure):
+    """rpp_gb_signature_job: one job of rpp_gb_signature_group."""
+
+    _fields_ = [
+        ("plan", ctypes.c_void_p),
+        ("dtype", ctypes.c_int32),
+        ("threads", ctypes.c_int32),
+        ("incr", ctypes.c_void_p),
+        ("offsets", ctypes.c_void_p),
+        ("length", ctypes.c_int64),
+        ("batch", ctypes.c_int64),
+        ("sig", ctypes.c_void_p),
+        ("sig_stride", ctypes.c_int64),
+        ("seed", ctypes.c_void_p),
+        ("seed_stride", ctypes.c_int64),
+        ("grad", ctypes.c_void_p),
+    ]
+
+
 class VectorArg(ctypes.Structure):
     """rpp_gb_vector_arg: {data, stride, begin, size}."""
 
@@ -92,6 +111,7 @@ SIGNATURES = {
     "rpp_gb_signature_tune": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp,
                               ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)],
     "rpp_gb_signature_with_schedule": [_vp, _vp, _i32, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i32],
+    "rpp_gb_signature_group": [_vp, ctypes.POINTER(SignatureJobArg), _i32, _i32],
     "rpp_gb_exp_letter_vjp": [_vp, _vp, _i32, _vp, _i64, _vp, _i64, _vp, _i64, _i64],
 }
 RESTYPES = {"rpp_gb_last_error_string": ctypes.c_char_p, "rpp_gb_version": ctypes.c_char_p}

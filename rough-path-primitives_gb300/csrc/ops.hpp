@@ -182,10 +182,49 @@ constexpr int kScheduleCotangentGlobal = 1 << 26;
 // kScheduleMergedReverse: reverse steps with D barriers (the recovery of the
 // prefix beside the transposition of the cotangent chains) instead of 2D - 1.
 constexpr int kScheduleMergedReverse = 1 << 27;
+// Bits 28-30 = P - 1: P >= 2 splits each path's state over a cluster of P
+// CTAs by first letter (P <= 8 divides the width; one fused launch;
+// signature_split.cu);
+// with kScheduleForwardTopGlobal the top level then lives in the signature
+// and seed rows.
+constexpr int kScheduleClusterShift = 28;
 template <typename T>
 cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStream_t s,
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
                              const T* seed, int64_t seed_stride, T* grad, bool forward, int threads);
+
+// Split-state launch (kScheduleClusterShift): `mode` as launch_width's, CTA
+// size `threads`, `P` CTAs per cluster.
+template <typename T>
+cudaError_t launch_signature_split(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const T* incr,
+                                   PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
+                                   T* grad, int mode, int threads, int P);
+
+// Grouped signature launch (rpp_gb_signature_group): several jobs -- batches
+// of paths of different (width, depth) and precision, each with its own
+// inputs and outputs -- in one persistent launch.  Each path of job j is run
+// by a team of `threads` threads of a CTA (several teams per CTA when the
+// job's state is small), with the per-path code of launch_signature, so its
+// outputs equal those of a separate call with that CTA size.
+constexpr int kMaxGroupJobs = 8;
+struct SignatureJob {
+    Geometry g;
+    bool fp64;
+    int threads;  // team size (a multiple of 32, at least width * depth)
+    const void* incr;
+    PathBatch paths;
+    void* sig;
+    int64_t sig_stride;
+    const void* seed;
+    int64_t seed_stride;
+    void* grad;
+};
+// Refusal reasons beside the CUDA status.
+enum class GroupRefusal : int { None = 0, StateTooLarge = 1, TooManyPaths = 2 };
+// `schedule`: threads per CTA in bits 0-9 (at most 640; 0: 640) and
+// kScheduleMergedReverse.
+cudaError_t launch_signature_group(const DeviceInfo& dev, cudaStream_t s, const SignatureJob* jobs, int njobs,
+                                   int schedule, GroupRefusal* refusal);
 
 // Allocation-free signature launch: the ragged-batch scratch lives in a
 // fixed device array of the library (see signature.cu); refuses shapes whose

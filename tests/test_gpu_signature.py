@@ -419,3 +419,29 @@ def test_host_buffers_refusals():
     assert not err and err.code == pkg.ErrorCode.InvalidArgument
     with pytest.raises(ValueError):
         pkg.signature_host(st, None, incr.cuda(), basis, 2, length=4, out=out)
+
+
+@pytest.mark.parametrize("W,D,threads", [(4, 6, 128), (4, 6, 256), (8, 4, 128), (8, 4, 512), (16, 3, 128),
+                                         (16, 3, 256), (4, 7, 128), (8, 3, 64)])
+@pytest.mark.parametrize("ragged", [False, True])
+def test_fp32_forward_top_level_in_registers(orc, W, D, threads, ragged):
+    """FP32 forward-only calls with W a multiple of 4 keep the top level's rows
+    in registers (8 rows per thread at W = 4, 4 at W = 8, 2 at W = 16; W4 D7
+    at 128 threads has more rows than that and keeps the shared-memory form):
+    against the FP64 oracle at 1e-5."""
+    rng = np.random.default_rng(W * 100 + D * 10 + threads)
+    B, L = 9, 11
+    if ragged:
+        lengths = rng.integers(0, 2 * L, B)
+        offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    else:
+        offsets = np.arange(B + 1, dtype=np.int64) * L
+    incr = rng.normal(0, 1 / np.sqrt(L), (int(offsets[-1]), W))
+    basis = pkg.TensorBasis(W, D)
+    sig = torch.full((B, basis.size()), float("nan"), dtype=torch.float32, device="cuda")
+    err = pkg.signature(pkg.GB300Strategy(torch.float32), None, dev(incr, torch.float32), basis, B,
+                        length=None if ragged else L, offsets=dev(offsets, torch.int64) if ragged else None,
+                        out=sig, schedule=threads)
+    assert err, err.message
+    esig, _ = orc.signature(W, D, incr, offsets)
+    assert_close(host(sig), esig, TOL_F32, f"FP32 W{W} D{D} forward, {threads} threads")
