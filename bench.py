@@ -510,6 +510,34 @@ def workload_ragged(pkg, torch, args, peak):
                  "fp32_tflops": 2.0 * steps_total * step_fma(W, D) / (ms32 / 1e3) / 1e12})
 
 
+def workload_ragged_fp32(pkg, torch, args, peak):
+    """The FP32 half of the uneven-length workload on its own: W8 D4 forward,
+    lengths U{16..2048} (the first --batch paths of the 10,000; default all),
+    tuned unless --schedule pins a schedule."""
+    W, D = 8, 4
+    B = 10_000 if args.batch == BATCH else args.batch
+    rng = np.random.default_rng(2024)
+    lengths = rng.integers(16, 2049, 10_000)[:B]
+    offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    incr_h = rng.normal(0, 1, (offsets[-1], W)) / np.sqrt(np.repeat(lengths, lengths))[:, None]
+    basis = pkg.TensorBasis(W, D)
+    off_d = torch.from_numpy(offsets).cuda()
+    x32 = torch.from_numpy(incr_h).cuda().float()
+    st32 = pkg.GB300Strategy(torch.float32)
+    s32 = torch.empty(B, basis.size(), dtype=torch.float32, device="cuda")
+    sched = args.schedule
+    if sched is None:
+        err, sched, _ = pkg.signature_tune(st32, None, x32, basis, B, offsets=off_d, out=s32)
+        err.raise_if_failed()
+    ms = 1e3 * _time_launches(torch, lambda: pkg.signature(st32, None, x32, basis, B, offsets=off_d, out=s32,
+                                                           schedule=sched),
+                              args.steps, args.warmup, torch.cuda.current_stream())
+    flops = 2.0 * int(offsets[-1]) * step_fma(W, D)
+    _line("uneven-length signatures paths/sec (W8 D4, L~U[16,2048], FP32 forward)", B / (ms / 1e3), "paths/s", ms,
+          "f32", {"workload": f"ragged_fp32_w8_d4_b{B}", "schedule": sched, "total_increments": int(offsets[-1])},
+          extra={"fp32_tflops": flops / (ms / 1e3) / 1e12})
+
+
 def workload_mixed(pkg, torch, args, peak):
     """The large mixed-shape configuration: 16,384 paths of 64 increments
     N(0, 1/64) at width 2 / depth 12 and 16,384 at width 16 / depth 3, FP64,
@@ -621,10 +649,14 @@ def workload_fwd_bwd(pkg, torch, args, peak, W, D, B, L, name):
     ell = torch.rand(B, dim, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
     sig = torch.empty(B, dim, dtype=torch.float64, device="cuda")
     grad = torch.empty_like(incr)
-    err, threads, _ = pkg.signature_tune(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad)
-    err.raise_if_failed()
+    if args.schedule is not None:  # a pinned schedule (profiling captures)
+        threads = args.schedule
+    else:
+        err, threads, _ = pkg.signature_tune(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad)
+        err.raise_if_failed()
     ms = 1e3 * _time_launches(
-        torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad),
+        torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad,
+                                     schedule=args.schedule),
         args.steps, args.warmup, torch.cuda.current_stream())
     _line(f"signature fwd+bwd paths/sec (W{W} D{D} L{L} FP64)", B / (ms / 1e3), "paths/s", ms, "f64",
           {"workload": name, "batch": B, "length": L, "schedule": threads, "threads_per_cta": threads & 1023,
@@ -740,6 +772,8 @@ def run_workloads(args):
             workload_mixed(pkg, torch, args, peak)
         elif w == "fp32":
             workload_fp32(pkg, torch, args, peak)
+        elif w == "ragged_fp32":
+            workload_ragged_fp32(pkg, torch, args, peak)
         elif w == "lie_exp":
             workload_lie_exp(pkg, torch, args, peak)
         elif w == "shuffle":
@@ -782,7 +816,7 @@ def main():
                          "for profiling captures")
     ap.add_argument("--workload", default=None,
                     help="other configurations instead of the headline: ft_mul, logsig, ragged, w6d6, w2d12, "
-                         "w16d3, mixed, fp32, adjoints, shuffle, lie_exp or all (comma-separated)")
+                         "w16d3, mixed, fp32, ragged_fp32, adjoints, shuffle, lie_exp or all (comma-separated)")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # one process per GPU: relaunch this command under torch.distributed.run
