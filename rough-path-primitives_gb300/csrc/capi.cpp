@@ -17,6 +17,7 @@
 #include <mutex>
 #include <new>
 #include <tuple>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -369,6 +370,10 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
                     candidates[ncand++] = t | rpp_gb::kScheduleSplit | rpp_gb::kScheduleForwardTopGlobal |
                                           rpp_gb::kScheduleCotangentGlobal | (rev << rpp_gb::kScheduleReverseShift);
         }
+    // forward-only FP32: the kernel with one warp per first letter
+    if (std::is_same<T, float>::value && sig && !seed &&
+        rpp_gb::letter_warps_supported(plan->geometry.width, plan->geometry.depth))
+        candidates[ncand++] = 32 | rpp_gb::kScheduleLetterWarps;
     // a state split over a cluster of P CTAs by first letter (P divides the
     // width), for states whose tensor alone exceeds 48 KB
     const auto& geo = plan->geometry;

@@ -193,6 +193,14 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
                              const T* seed, int64_t seed_stride, T* grad, bool forward, int threads);
 
+// kScheduleLetterWarps (bit 16 of a forward-only FP32 call's schedule, where
+// bits 16-25 have no other use): the FP32 forward kernel with one warp per
+// first letter and compile-time (width, depth) (signature_fp32.cu).
+constexpr int kScheduleLetterWarps = 1 << 16;
+bool letter_warps_supported(int width, int depth);
+cudaError_t launch_signature_letters(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const float* incr,
+                                     PathBatch paths, float* sig, int64_t sig_stride);
+
 // Split-state launch (kScheduleClusterShift): `mode` as launch_width's, CTA
 // size `threads`, `P` CTAs per cluster.
 template <typename T>

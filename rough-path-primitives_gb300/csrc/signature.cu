@@ -149,6 +149,11 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
                          PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride, T* grad,
                          int mode, int schedule) {
     const bool bwd = mode & kBackward;
+    if constexpr (std::is_same<T, float>::value) {
+        // forward-only FP32 with one warp per first letter (signature_fp32.cu)
+        if (schedule > 0 && (schedule & kScheduleLetterWarps) && mode == (kForward | kTopLevel))
+            return launch_signature_letters(sg.g, dev, s, incr, paths, sig, sig_stride);
+    }
     const int cluster = schedule > 0 ? ((schedule >> kScheduleClusterShift) & 7) + 1 : 1;
     if (cluster >= 2) {  // the state split over a cluster of CTAs (signature_split.cu)
         // kScheduleForwardTopGlobal: the top level in the signature / seed

@@ -1,0 +1,295 @@
+// signature_fp32.cu -- FP32 forward signatures with one warp per first letter
+// (schedule bit 16 on forward-only calls, kScheduleLetterWarps).
+//
+// The same Chen step as signature_body.cuh (Horner chains
+// T^n_j = S_j + T^n_{j-1} (x) x / (n-j+1), S_n <- T^n_n), organised for FP32,
+// where the shared-memory kernel is bound by instruction issue (about twelve
+// instructions per FFMA at W8 D4: the loop and index bookkeeping of the small
+// lower levels and a CTA barrier per stage).  Here:
+//  * A CTA of W warps runs one path; warp c holds the coefficients whose
+//    first letter is c (W^{j-1} of level j).  A coefficient's Horner parent is
+//    its prefix, which has the same first letter, so the warps never exchange
+//    data during the path (the slicing of the cluster-split kernel, at warp
+//    granularity).
+//  * Each lane evaluates the Horner chains of its own coefficients from the
+//    old lower levels (letter_step): no chain arrays and no stage barriers,
+//    two __syncwarp per step.
+//  * Width and depth are compile-time, so every stage, chain offset, level
+//    size and index split is a constant and the loops unroll.
+//  * The top level lives in registers: lane l holds the rows l, l + 32, ... of
+//    the warp's slice (W coefficients sharing one prefix), so one shared load of
+//    T^D_{D-1}[row] serves W FMAs with the increment in registers.  No chain
+//    reads the top level, so no other thread needs it.
+//  * The scaled increments x_a / m (m = 1..D) are one value per lane
+//    (D*W <= 32), double-buffered by step parity; each lane's letter is
+//    loaded eight steps ahead into a register ring (a step here is short,
+//    and a load one step ahead left the L2 latency exposed).
+// The arithmetic is the shared-memory kernel's (the same chains and scale
+// factors), summed in the same order per coefficient.
+#include "signature_body.cuh"
+
+namespace rpp_gb {
+namespace {
+
+// W^n as a loop, not a recursion: inlined into the unrolled stage loops it
+// folds to a constant, so the index splits below are multiply-shifts (a
+// recursive form was not inlined, leaving run-time divisions in every step).
+constexpr uint32_t cpow(uint32_t w, int n) {
+    uint32_t r = 1;
+    for (int i = 0; i < n; ++i) r *= w;
+    return r;
+}
+
+// Per-warp layout (floats): the slices of levels 1..D-1 and two buffers of
+// scaled increments.
+template <int W, int D>
+struct LetterLayout {
+    static constexpr uint32_t slice(int j) { return cpow(W, j - 1); }  // level j >= 1
+    static constexpr uint32_t s_off(int j) {                            // level j in S, 1 <= j < D
+        uint32_t o = 0;
+        for (int i = 1; i < j; ++i) o += slice(i);
+        return o;
+    }
+    static constexpr uint32_t s_size = s_off(D);
+    static constexpr uint32_t xcs = D * W;  // one increment buffer
+    static constexpr uint32_t warp_floats = s_size + 2 * xcs;
+    static constexpr uint32_t top_rows = slice(D - 1);                      // rows of W on top
+    static constexpr int rows_per_lane = static_cast<int>((top_rows + 31) / 32);
+};
+
+// Full tensor level start db[j] = (W^j - 1) / (W - 1) (W >= 2).
+template <int W>
+constexpr uint32_t level_start(int j) {
+    uint32_t s = 0;
+    for (int i = 0; i < j; ++i) s += cpow(W, i);
+    return s;
+}
+
+// Lower-level coefficients (levels 1..D-1 of the warp's slice) a lane
+// updates per step: ceil(W^{n-1} / 32) of level n.
+template <int W, int D>
+constexpr int lower_per_lane() {
+    int t = 0;
+    for (int n = 1; n < D; ++n) t += static_cast<int>((cpow(W, n - 1) + 31) / 32);
+    return t;
+}
+
+// One forward step of warp c (its first-letter slice).  Every coefficient's
+// Horner chain is evaluated by the lane that updates it, from the old lower
+// levels: for a word (c, a_2, ..., a_n) of level n,
+//     T_1 = S_1 + x_c / n,   T_j = S_j[a_1..a_j] + T_{j-1} x_{a_j} / (n-j+1),
+// and the new S_n is T_n (the top level adds T_{D-1} x_a to its registers).
+// These are the shared-memory kernel's chain values, formed by the same fused
+// multiply-adds in the same order, so the results are identical; only the
+// sharing of a prefix's chain value between coefficients is given up (17 %
+// more FMAs at W8 D4), for no chain arrays, no stage barriers and little
+// index arithmetic.  All lanes read the old levels before any lane writes the
+// new ones (one __syncwarp between); the caller's __syncwarp after refreshing
+// the increment orders the writes before the next step's reads.
+template <int W, int D>
+__device__ __forceinline__ void letter_step(float* S, const float* xc,
+                                            float (&top)[LetterLayout<W, D>::rows_per_lane][W], uint32_t c,
+                                            uint32_t lane) {
+    using Lay = LetterLayout<W, D>;
+    constexpr int R = Lay::rows_per_lane;
+    const float s1 = S[Lay::s_off(1)];
+    float t1[D + 1];  // T^n_1 = S_1 + S_0 x_c / n (S_0 = 1)
+#pragma unroll
+    for (int n = 2; n <= D; ++n) t1[n] = s1 + xc[(n - 1) * W + c];
+    float nv[lower_per_lane<W, D>() > 0 ? lower_per_lane<W, D>() : 1];
+    int v = 0;
+    // level 1: S_1 + S_0 x_c
+    nv[v++] = s1 + xc[c];
+#pragma unroll
+    for (int n = 2; n < D; ++n) {
+        const uint32_t sl = Lay::slice(n);
+#pragma unroll
+        for (uint32_t q = 0; q < (sl + 31) / 32; ++q, ++v) {
+            const uint32_t u = lane + 32u * q;
+            if (u < sl) {
+                float acc = t1[n];
+#pragma unroll
+                for (int j = 2; j <= n; ++j) {
+                    const uint32_t pref = u / cpow(W, n - j);  // index of (c, a_2..a_j) in level j's slice
+                    acc = fmaf(acc, xc[(n - j) * W + pref % W], S[Lay::s_off(j) + pref]);
+                }
+                nv[v] = acc;
+            }
+        }
+    }
+    // the top level: rows (c, a_2..a_{D-1}) of W coefficients
+    float x1[W];
+#pragma unroll
+    for (int a = 0; a < W; ++a) x1[a] = xc[a];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t row = lane + 32u * r;
+        if (row < Lay::top_rows) {
+            float acc = t1[D];
+#pragma unroll
+            for (int j = 2; j < D; ++j) {
+                const uint32_t pref = row / cpow(W, D - 1 - j);
+                acc = fmaf(acc, xc[(D - j) * W + pref % W], S[Lay::s_off(j) + pref]);
+            }
+#pragma unroll
+            for (int a = 0; a < W; ++a) top[r][a] = fmaf(acc, x1[a], top[r][a]);
+        }
+    }
+    __syncwarp();  // every lane has read the old levels
+    v = 0;
+    if (lane == 0) S[Lay::s_off(1)] = nv[0];
+    ++v;
+#pragma unroll
+    for (int n = 2; n < D; ++n) {
+        const uint32_t sl = Lay::slice(n);
+#pragma unroll
+        for (uint32_t q = 0; q < (sl + 31) / 32; ++q, ++v) {
+            const uint32_t u = lane + 32u * q;
+            if (u < sl) S[Lay::s_off(n) + u] = nv[v];
+        }
+    }
+}
+
+// CTAs per SM the register budget is sized for: 32 warps per SM (64
+// registers a thread), or 20 (about 100 registers) for the shapes whose
+// lower levels and top rows spilled at 64 (W5 D5, W3 D6).
+constexpr int letter_min_blocks(int W, int D) {
+    return ((W == 5 && D == 5) || (W == 3 && D == 6)) ? 640 / (W * 32) : 1024 / (W * 32);
+}
+
+template <int W, int D>
+__global__ void __launch_bounds__(W * 32, letter_min_blocks(W, D)) k_signature_letters(const float* __restrict__ incr, PathBatch paths,
+                                                              float* sig, int64_t sig_stride) {
+    using Lay = LetterLayout<W, D>;
+    static_assert(D >= 2 && D * W <= 32, "one scaled increment per lane");
+    static_assert(LetterLayout<W, D>::rows_per_lane * W <= 32, "at most 32 registers of top-level rows");
+    constexpr int R = Lay::rows_per_lane;
+    constexpr int PF = 8;  // increments prefetched ahead
+    extern __shared__ __align__(16) float sm_letters[];
+    __shared__ int64_t s_next;
+    const uint32_t c = threadIdx.x / 32;  // this warp's first letter
+    const uint32_t lane = threadIdx.x % 32;
+    float* S = sm_letters + c * Lay::warp_floats;
+    float* xcb = S + Lay::s_size;
+    // the scaled increment this lane holds: letter lane % W over m = lane / W + 1
+    const bool xlane = lane < static_cast<uint32_t>(D * W);
+    const float inv_m = xlane ? 1.0f / static_cast<float>(lane / W + 1) : 0.0f;
+
+    int64_t slot = blockIdx.x;
+    if (paths.counter) {
+        if (threadIdx.x == 0) s_next = static_cast<int64_t>(atomicAdd(paths.counter, 1u));
+        __syncthreads();
+        slot = s_next;
+        __syncthreads();
+    }
+    while (slot < paths.batch) {
+        const int64_t b = paths.order ? paths.order[slot] : slot;
+        const int64_t off = paths.offsets ? paths.offsets[b] : b * paths.length;
+        const int64_t len = paths.offsets ? paths.offsets[b + 1] - off : paths.length;
+        const float* xin = incr + off * W;
+        for (uint32_t i = lane; i < Lay::s_size; i += 32) S[i] = 0.0f;
+        float top[R][W];
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+#pragma unroll
+            for (int a = 0; a < W; ++a) top[i][a] = 0.0f;
+        // prefetch ring: xr[q] holds this lane's letter of increment k0 + q
+        // for the block of PF steps starting at k0 (loads issued PF steps
+        // ahead, so their L2 latency is hidden behind PF short steps)
+        float xr[PF];
+#pragma unroll
+        for (int q = 0; q < PF; ++q) xr[q] = (xlane && q < len) ? __ldg(xin + q * W + lane % W) : 0.0f;
+        if (xlane && len > 0) xcb[lane] = xr[0] * inv_m;
+        __syncwarp();
+        for (int64_t k0 = 0; k0 < len; k0 += PF) {
+#pragma unroll
+            for (int q = 0; q < PF; ++q) {
+                const int64_t k = k0 + q;
+                if (k >= len) break;
+                // slot q has been consumed (x_k is in the increment buffer):
+                // refill it with x_{k+PF}
+                if (xlane && k + PF < len) xr[q] = __ldg(xin + (k + PF) * W + lane % W);
+                letter_step<W, D>(S, xcb + (k & 1) * Lay::xcs, top, c, lane);
+                if (xlane && k + 1 < len) xcb[((k + 1) & 1) * Lay::xcs + lane] = xr[(q + 1) % PF] * inv_m;
+                __syncwarp();
+            }
+        }
+        // the signature row: S_0 (warp 0), the slices of levels 1..D-1 and
+        // the top rows
+        float* dst = sig + b * sig_stride;
+        if (c == 0 && lane == 0) dst[0] = 1.0f;
+#pragma unroll
+        for (int j = 1; j < D; ++j) {
+            const uint32_t sl = Lay::slice(j);
+            for (uint32_t u = lane; u < sl; u += 32) dst[level_start<W>(j) + c * sl + u] = S[Lay::s_off(j) + u];
+        }
+        float* dtop = dst + level_start<W>(D) + c * Lay::slice(D);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t row = lane + 32u * r;
+            if (row < Lay::top_rows)
+#pragma unroll
+                for (int a = 0; a < W; ++a) dtop[row * W + a] = top[r][a];
+        }
+        __syncwarp();
+        if (paths.counter) {
+            __syncthreads();  // every warp has read s_next
+            if (threadIdx.x == 0) s_next = static_cast<int64_t>(atomicAdd(paths.counter, 1u));
+            __syncthreads();
+            slot = s_next;
+        } else {
+            slot += gridDim.x;
+        }
+    }
+}
+
+template <int W, int D>
+cudaError_t launch_letters_shape(const DeviceInfo& dev, cudaStream_t s, const float* incr, PathBatch paths,
+                                 float* sig, int64_t sig_stride) {
+    using Lay = LetterLayout<W, D>;
+    constexpr auto kernel = k_signature_letters<W, D>;
+    const size_t smem = static_cast<size_t>(W) * Lay::warp_floats * sizeof(float);
+    dim3 grid;
+    cudaError_t err = batch_grid(kernel, dev, W * 32, smem, paths.batch, grid);
+    if (err != cudaSuccess) return err;
+    kernel<<<grid, W * 32, smem, s>>>(incr, paths, sig, sig_stride);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Instantiated shapes: D*W <= 32 (one scaled increment per lane), at most 32
+// registers of top-level rows per lane, and few enough lower-level
+// coefficients per lane to stay within 64 registers (W4 D6 and W3 D7 needed
+// 168).
+bool letter_warps_supported(int width, int depth) {
+    switch (width * 100 + depth) {
+        case 802: case 803: case 804: case 502: case 503: case 504: case 505: case 404: case 405:
+        case 604: case 305: case 306: case 1602:
+            return true;
+        default:
+            return false;
+    }
+}
+
+cudaError_t launch_signature_letters(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const float* incr,
+                                     PathBatch paths, float* sig, int64_t sig_stride) {
+    switch (g.width * 100 + g.depth) {
+        case 802: return launch_letters_shape<8, 2>(dev, s, incr, paths, sig, sig_stride);
+        case 803: return launch_letters_shape<8, 3>(dev, s, incr, paths, sig, sig_stride);
+        case 804: return launch_letters_shape<8, 4>(dev, s, incr, paths, sig, sig_stride);
+        case 502: return launch_letters_shape<5, 2>(dev, s, incr, paths, sig, sig_stride);
+        case 503: return launch_letters_shape<5, 3>(dev, s, incr, paths, sig, sig_stride);
+        case 504: return launch_letters_shape<5, 4>(dev, s, incr, paths, sig, sig_stride);
+        case 505: return launch_letters_shape<5, 5>(dev, s, incr, paths, sig, sig_stride);
+        case 404: return launch_letters_shape<4, 4>(dev, s, incr, paths, sig, sig_stride);
+        case 405: return launch_letters_shape<4, 5>(dev, s, incr, paths, sig, sig_stride);
+        case 604: return launch_letters_shape<6, 4>(dev, s, incr, paths, sig, sig_stride);
+        case 305: return launch_letters_shape<3, 5>(dev, s, incr, paths, sig, sig_stride);
+        case 306: return launch_letters_shape<3, 6>(dev, s, incr, paths, sig, sig_stride);
+        case 1602: return launch_letters_shape<16, 2>(dev, s, incr, paths, sig, sig_stride);
+        default: return cudaErrorInvalidConfiguration;
+    }
+}
+
+}  // namespace rpp_gb

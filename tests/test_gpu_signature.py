@@ -272,10 +272,11 @@ def test_autotuner_records_schedule_and_keeps_parity(orc):
     # schedule: threads per CTA in bits 0-9, CTA-per-SM cap in bits 10-13,
     # bit 14 for the two-launch form (bit 15: its forward top level in global
     # memory; bits 16-25: its reverse launch's own CTA size), bit 26 for the
-    # cotangent arrays in a global workspace
+    # cotangent arrays in a global workspace, bit 27 for the D-barrier reverse
+    # step; no cluster split for a state this small (bits 28-30)
     sizes = (128, 192, 256, 320, 384, 512)
     assert (threads & 1023) in sizes and ((threads >> 10) & 15) in (0, 2, 3)
-    assert (threads >> 27) == 0 and ((threads >> 16) & 1023) in (0,) + sizes
+    assert (threads >> 28) == 0 and ((threads >> 16) & 1023) in (0,) + sizes
     assert ((threads >> 16) & 1023) == 0 or threads & (1 << 14)
     assert ms > 0
     esig, egrad = orc.signature(W, D, incr, np.arange(B + 1) * L, ell=ell)
@@ -445,3 +446,36 @@ def test_fp32_forward_top_level_in_registers(orc, W, D, threads, ragged):
     assert err, err.message
     esig, _ = orc.signature(W, D, incr, offsets)
     assert_close(host(sig), esig, TOL_F32, f"FP32 W{W} D{D} forward, {threads} threads")
+
+
+@pytest.mark.parametrize("W,D", [(8, 4), (8, 2), (5, 5), (5, 3), (4, 5), (6, 4), (3, 6), (16, 2)])
+@pytest.mark.parametrize("ragged", [False, True])
+def test_fp32_forward_one_warp_per_letter(orc, W, D, ragged):
+    """The FP32 forward kernel with one warp per first letter and compile-time
+    (width, depth) (schedule bit 16 on a forward-only call): against the FP64
+    oracle at 1e-5, equal-length and ragged with empty and unit paths."""
+    rng = np.random.default_rng(W * 37 + D)
+    B, L = 13, 9
+    if ragged:
+        lengths = np.array([0, 1, 2, 17, 5, 0, 9, 31, 1, 4, 12, 3, 8])
+        offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    else:
+        offsets = np.arange(B + 1, dtype=np.int64) * L
+    incr = rng.normal(0, 1 / np.sqrt(L), (int(offsets[-1]), W))
+    basis = pkg.TensorBasis(W, D)
+    sig = torch.full((B, basis.size()), float("nan"), dtype=torch.float32, device="cuda")
+    err = pkg.signature(pkg.GB300Strategy(torch.float32), None, dev(incr, torch.float32), basis, B,
+                        length=None if ragged else L, offsets=dev(offsets, torch.int64) if ragged else None,
+                        out=sig, schedule=32 | (1 << 16))
+    assert err, err.message
+    esig, _ = orc.signature(W, D, incr, offsets)
+    assert_close(host(sig), esig, TOL_F32, f"FP32 letter warps W{W} D{D}")
+
+
+def test_fp32_one_warp_per_letter_refuses_other_shapes():
+    basis = pkg.TensorBasis(7, 4)  # not instantiated
+    x = torch.zeros(6, 7, dtype=torch.float32, device="cuda")
+    sig = torch.empty(2, basis.size(), dtype=torch.float32, device="cuda")
+    err = pkg.signature(pkg.GB300Strategy(torch.float32), None, x, basis, 2, length=3, out=sig,
+                        schedule=32 | (1 << 16))
+    assert not err
