@@ -17,13 +17,16 @@
 //  * Width and depth are compile-time, so every stage, chain offset, level
 //    size and index split is a constant and the loops unroll.
 //  * The top level lives in registers: lane l holds the rows l, l + 32, ... of
-//    the warp's slice (W coefficients sharing one prefix), so one shared load of
-//    T^D_{D-1}[row] serves W FMAs with the increment in registers.  No chain
-//    reads the top level, so no other thread needs it.
-//  * The scaled increments x_a / m (m = 1..D) are one value per lane
-//    (D*W <= 32), double-buffered by step parity; each lane's letter is
-//    loaded eight steps ahead into a register ring (a step here is short,
-//    and a load one step ahead left the L2 latency exposed).
+//    the warp's slice (W coefficients sharing one prefix), so one chain value
+//    serves W FMAs with the increment in registers.  No chain reads the top
+//    level, so no other thread needs it.  Level D-1 lives in registers too:
+//    lane l holds its coefficients l, l + 32, ..., which are exactly the
+//    prefixes of its top rows and are read by no other lane.
+//  * The increment's W letters are double-buffered by step parity in shared
+//    memory; x_a / m is formed in a register as x_a * (1/m), the single
+//    rounding the shared-memory kernel's scaled increments get.  Each lane
+//    a < W loads its letter eight steps ahead into a register ring (a step
+//    here is short, and a load one step ahead left the L2 latency exposed).
 // The arithmetic is the shared-memory kernel's (the same chains and scale
 // factors), summed in the same order per coefficient.
 #include "signature_body.cuh"
@@ -40,19 +43,24 @@ constexpr uint32_t cpow(uint32_t w, int n) {
     return r;
 }
 
-// Per-warp layout (floats): the slices of levels 1..D-1 and two buffers of
-// scaled increments.
+// Per-warp layout (floats): two buffers of scaled increments (each padded to
+// a multiple of four floats, so the top's W letters load as float4), then the
+// slices of the levels kept in shared memory, 1..D-2 (level D-1 lives in
+// registers; at D = 2 level 1 stays in shared memory).  Each warp's region is a
+// multiple of four floats, so every buffer starts on a 16-byte boundary.
 template <int W, int D>
 struct LetterLayout {
     static constexpr uint32_t slice(int j) { return cpow(W, j - 1); }  // level j >= 1
-    static constexpr uint32_t s_off(int j) {                            // level j in S, 1 <= j < D
+    static constexpr uint32_t s_off(int j) {                            // level j in S, 1 <= j
         uint32_t o = 0;
         for (int i = 1; i < j; ++i) o += slice(i);
         return o;
     }
-    static constexpr uint32_t s_size = s_off(D);
-    static constexpr uint32_t xcs = D * W;  // one increment buffer
-    static constexpr uint32_t warp_floats = s_size + 2 * xcs;
+    static constexpr bool reg_dm1 = D >= 3;                // level D-1 in registers
+    static constexpr int smem_levels = reg_dm1 ? D - 2 : D - 1;
+    static constexpr uint32_t s_size = s_off(smem_levels + 1);
+    static constexpr uint32_t xcs = (W + 3) / 4 * 4;       // one increment buffer (x_a)
+    static constexpr uint32_t warp_floats = (2 * xcs + s_size + 3) / 4 * 4;
     static constexpr uint32_t top_rows = slice(D - 1);                      // rows of W on top
     static constexpr int rows_per_lane = static_cast<int>((top_rows + 31) / 32);
 };
@@ -70,7 +78,7 @@ constexpr uint32_t level_start(int j) {
 template <int W, int D>
 constexpr int lower_per_lane() {
     int t = 0;
-    for (int n = 1; n < D; ++n) t += static_cast<int>((cpow(W, n - 1) + 31) / 32);
+    for (int n = 1; n <= LetterLayout<W, D>::smem_levels; ++n) t += static_cast<int>((cpow(W, n - 1) + 31) / 32);
     return t;
 }
 
@@ -87,21 +95,29 @@ constexpr int lower_per_lane() {
 // new ones (one __syncwarp between); the caller's __syncwarp after refreshing
 // the increment orders the writes before the next step's reads.
 template <int W, int D>
-__device__ __forceinline__ void letter_step(float* S, const float* xc,
-                                            float (&top)[LetterLayout<W, D>::rows_per_lane][W], uint32_t c,
+__device__ __forceinline__ void letter_step(float* S, const float* x,
+                                            float (&top)[LetterLayout<W, D>::rows_per_lane][W],
+                                            float (&sd)[LetterLayout<W, D>::rows_per_lane], uint32_t c,
                                             uint32_t lane) {
     using Lay = LetterLayout<W, D>;
     constexpr int R = Lay::rows_per_lane;
-    const float s1 = S[Lay::s_off(1)];
+    constexpr int NS = Lay::smem_levels;  // levels in shared memory: 1..NS
+    // x_a / m is formed in a register as x_a * (1/m) with __fmul_rn: the one
+    // rounding the shared-memory kernel's scaled increments get (1/m is the
+    // correctly rounded constant, as that kernel's 1/m table is), and no
+    // contraction of the product into a following add
+    const float s1 = NS >= 1 ? S[Lay::s_off(1)] : 0.0f;
+    const float xcc = x[c];
     float t1[D + 1];  // T^n_1 = S_1 + S_0 x_c / n (S_0 = 1)
 #pragma unroll
-    for (int n = 2; n <= D; ++n) t1[n] = s1 + xc[(n - 1) * W + c];
+    for (int n = 2; n <= D; ++n) t1[n] = s1 + __fmul_rn(xcc, 1.0f / static_cast<float>(n));
     float nv[lower_per_lane<W, D>() > 0 ? lower_per_lane<W, D>() : 1];
     int v = 0;
     // level 1: S_1 + S_0 x_c
-    nv[v++] = s1 + xc[c];
+    nv[v++] = s1 + xcc;
+    // levels 2..NS in shared memory
 #pragma unroll
-    for (int n = 2; n < D; ++n) {
+    for (int n = 2; n <= NS; ++n) {
         const uint32_t sl = Lay::slice(n);
 #pragma unroll
         for (uint32_t q = 0; q < (sl + 31) / 32; ++q, ++v) {
@@ -111,28 +127,51 @@ __device__ __forceinline__ void letter_step(float* S, const float* xc,
 #pragma unroll
                 for (int j = 2; j <= n; ++j) {
                     const uint32_t pref = u / cpow(W, n - j);  // index of (c, a_2..a_j) in level j's slice
-                    acc = fmaf(acc, xc[(n - j) * W + pref % W], S[Lay::s_off(j) + pref]);
+                    const float xm = __fmul_rn(x[pref % W], 1.0f / static_cast<float>(n - j + 1));
+                    acc = fmaf(acc, xm, S[Lay::s_off(j) + pref]);
                 }
                 nv[v] = acc;
             }
         }
     }
-    // the top level: rows (c, a_2..a_{D-1}) of W coefficients
+    // level D-1 in registers (lane owns coefficients lane + 32 r, which are
+    // also the prefixes of its top rows) and the top rows
     float x1[W];
+    if constexpr (W % 4 == 0) {
 #pragma unroll
-    for (int a = 0; a < W; ++a) x1[a] = xc[a];
+        for (int a = 0; a < W; a += 4) {
+            const float4 x4 = *reinterpret_cast<const float4*>(x + a);
+            x1[a] = x4.x;
+            x1[a + 1] = x4.y;
+            x1[a + 2] = x4.z;
+            x1[a + 3] = x4.w;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < W; ++a) x1[a] = x[a];
+    }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const uint32_t row = lane + 32u * r;
         if (row < Lay::top_rows) {
-            float acc = t1[D];
+            // chains T^{D-1} (the new S_{D-1}) and T^D along the row's prefixes
+            float accd = t1[D];
+            float accm = t1[D - 1];
 #pragma unroll
-            for (int j = 2; j < D; ++j) {
+            for (int j = 2; j < D - 1; ++j) {
                 const uint32_t pref = row / cpow(W, D - 1 - j);
-                acc = fmaf(acc, xc[(D - j) * W + pref % W], S[Lay::s_off(j) + pref]);
+                const float sj = S[Lay::s_off(j) + pref];
+                const float xp = x[pref % W];
+                accd = fmaf(accd, __fmul_rn(xp, 1.0f / static_cast<float>(D - j + 1)), sj);
+                accm = fmaf(accm, __fmul_rn(xp, 1.0f / static_cast<float>(D - j)), sj);
+            }
+            if constexpr (Lay::reg_dm1) {
+                const float xa = x[row % W];
+                accd = fmaf(accd, __fmul_rn(xa, 0.5f), sd[r]);  // T^D_{D-1}: old S_{D-1}
+                sd[r] = fmaf(accm, xa, sd[r]);       // new S_{D-1} = T^{D-1}_{D-1}
             }
 #pragma unroll
-            for (int a = 0; a < W; ++a) top[r][a] = fmaf(acc, x1[a], top[r][a]);
+            for (int a = 0; a < W; ++a) top[r][a] = fmaf(accd, x1[a], top[r][a]);
         }
     }
     __syncwarp();  // every lane has read the old levels
@@ -140,7 +179,7 @@ __device__ __forceinline__ void letter_step(float* S, const float* xc,
     if (lane == 0) S[Lay::s_off(1)] = nv[0];
     ++v;
 #pragma unroll
-    for (int n = 2; n < D; ++n) {
+    for (int n = 2; n <= NS; ++n) {
         const uint32_t sl = Lay::slice(n);
 #pragma unroll
         for (uint32_t q = 0; q < (sl + 31) / 32; ++q, ++v) {
@@ -161,7 +200,7 @@ template <int W, int D>
 __global__ void __launch_bounds__(W * 32, letter_min_blocks(W, D)) k_signature_letters(const float* __restrict__ incr, PathBatch paths,
                                                               float* sig, int64_t sig_stride) {
     using Lay = LetterLayout<W, D>;
-    static_assert(D >= 2 && D * W <= 32, "one scaled increment per lane");
+    static_assert(D >= 2 && W <= 32, "one letter per lane");
     static_assert(LetterLayout<W, D>::rows_per_lane * W <= 32, "at most 32 registers of top-level rows");
     constexpr int R = Lay::rows_per_lane;
     constexpr int PF = 8;  // increments prefetched ahead
@@ -169,11 +208,10 @@ __global__ void __launch_bounds__(W * 32, letter_min_blocks(W, D)) k_signature_l
     __shared__ int64_t s_next;
     const uint32_t c = threadIdx.x / 32;  // this warp's first letter
     const uint32_t lane = threadIdx.x % 32;
-    float* S = sm_letters + c * Lay::warp_floats;
-    float* xcb = S + Lay::s_size;
-    // the scaled increment this lane holds: letter lane % W over m = lane / W + 1
-    const bool xlane = lane < static_cast<uint32_t>(D * W);
-    const float inv_m = xlane ? 1.0f / static_cast<float>(lane / W + 1) : 0.0f;
+    float* xcb = sm_letters + c * Lay::warp_floats;  // two increment buffers
+    float* S = xcb + 2 * Lay::xcs;                  // levels 1..smem_levels
+    // lane a < W holds letter a of the increments
+    const bool xlane = lane < static_cast<uint32_t>(W);
 
     int64_t slot = blockIdx.x;
     if (paths.counter) {
@@ -189,17 +227,20 @@ __global__ void __launch_bounds__(W * 32, letter_min_blocks(W, D)) k_signature_l
         const float* xin = incr + off * W;
         for (uint32_t i = lane; i < Lay::s_size; i += 32) S[i] = 0.0f;
         float top[R][W];
+        float sd[R];  // this lane's coefficients of level D-1 (when in registers)
 #pragma unroll
-        for (int i = 0; i < R; ++i)
+        for (int i = 0; i < R; ++i) {
+            sd[i] = 0.0f;
 #pragma unroll
             for (int a = 0; a < W; ++a) top[i][a] = 0.0f;
+        }
         // prefetch ring: xr[q] holds this lane's letter of increment k0 + q
         // for the block of PF steps starting at k0 (loads issued PF steps
         // ahead, so their L2 latency is hidden behind PF short steps)
         float xr[PF];
 #pragma unroll
-        for (int q = 0; q < PF; ++q) xr[q] = (xlane && q < len) ? __ldg(xin + q * W + lane % W) : 0.0f;
-        if (xlane && len > 0) xcb[lane] = xr[0] * inv_m;
+        for (int q = 0; q < PF; ++q) xr[q] = (xlane && q < len) ? __ldg(xin + q * W + lane) : 0.0f;
+        if (xlane && len > 0) xcb[lane] = xr[0];
         __syncwarp();
         for (int64_t k0 = 0; k0 < len; k0 += PF) {
 #pragma unroll
@@ -208,9 +249,9 @@ __global__ void __launch_bounds__(W * 32, letter_min_blocks(W, D)) k_signature_l
                 if (k >= len) break;
                 // slot q has been consumed (x_k is in the increment buffer):
                 // refill it with x_{k+PF}
-                if (xlane && k + PF < len) xr[q] = __ldg(xin + (k + PF) * W + lane % W);
-                letter_step<W, D>(S, xcb + (k & 1) * Lay::xcs, top, c, lane);
-                if (xlane && k + 1 < len) xcb[((k + 1) & 1) * Lay::xcs + lane] = xr[(q + 1) % PF] * inv_m;
+                if (xlane && k + PF < len) xr[q] = __ldg(xin + (k + PF) * W + lane);
+                letter_step<W, D>(S, xcb + (k & 1) * Lay::xcs, top, sd, c, lane);
+                if (xlane && k + 1 < len) xcb[((k + 1) & 1) * Lay::xcs + lane] = xr[(q + 1) % PF];
                 __syncwarp();
             }
         }
@@ -219,17 +260,20 @@ __global__ void __launch_bounds__(W * 32, letter_min_blocks(W, D)) k_signature_l
         float* dst = sig + b * sig_stride;
         if (c == 0 && lane == 0) dst[0] = 1.0f;
 #pragma unroll
-        for (int j = 1; j < D; ++j) {
+        for (int j = 1; j <= Lay::smem_levels; ++j) {
             const uint32_t sl = Lay::slice(j);
             for (uint32_t u = lane; u < sl; u += 32) dst[level_start<W>(j) + c * sl + u] = S[Lay::s_off(j) + u];
         }
+        float* ddm1 = dst + level_start<W>(D - 1) + c * Lay::slice(D - 1);
         float* dtop = dst + level_start<W>(D) + c * Lay::slice(D);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const uint32_t row = lane + 32u * r;
-            if (row < Lay::top_rows)
+            if (row < Lay::top_rows) {
+                if constexpr (Lay::reg_dm1) ddm1[row] = sd[r];
 #pragma unroll
                 for (int a = 0; a < W; ++a) dtop[row * W + a] = top[r][a];
+            }
         }
         __syncwarp();
         if (paths.counter) {
@@ -258,10 +302,9 @@ cudaError_t launch_letters_shape(const DeviceInfo& dev, cudaStream_t s, const fl
 
 }  // namespace
 
-// Instantiated shapes: D*W <= 32 (one scaled increment per lane), at most 32
-// registers of top-level rows per lane, and few enough lower-level
-// coefficients per lane to stay within 64 registers (W4 D6 and W3 D7 needed
-// 168).
+// Instantiated shapes: at most 32 registers of top-level rows per lane, and
+// few enough lower-level coefficients per lane to stay within 64 registers
+// (W4 D6 and W3 D7 needed 168 in an earlier form).
 bool letter_warps_supported(int width, int depth) {
     switch (width * 100 + depth) {
         case 802: case 803: case 804: case 502: case 503: case 504: case 505: case 404: case 405:

@@ -479,3 +479,28 @@ def test_fp32_one_warp_per_letter_refuses_other_shapes():
     err = pkg.signature(pkg.GB300Strategy(torch.float32), None, x, basis, 2, length=3, out=sig,
                         schedule=32 | (1 << 16))
     assert not err
+
+
+@pytest.mark.parametrize("W,D", [(8, 4), (5, 5), (4, 5), (6, 4), (3, 6)])
+def test_fp32_one_warp_per_letter_equals_shared_memory_kernel(W, D):
+    """The warp-per-letter kernel forms the same fused multiply-adds in the same
+    order as the shared-memory kernel (each chain value recomputed by the lane
+    that needs it; x/m rounded once, as the kernel's scaled increments are), so
+    the two agree bit for bit."""
+    rng = np.random.default_rng(W * 7 + D)
+    lengths = rng.integers(0, 40, 21)
+    offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    incr = dev(rng.normal(0, 0.3, (int(offsets[-1]), W)), torch.float32)
+    offs = dev(offsets, torch.int64)
+    basis = pkg.TensorBasis(W, D)
+    st = pkg.GB300Strategy(torch.float32)
+    out = []
+    for schedule in (32 | (1 << 16), 128, 256 | (2 << 10)):
+        sig = torch.full((len(lengths), basis.size()), float("nan"), dtype=torch.float32, device="cuda")
+        err = pkg.signature(st, None, incr, basis, len(lengths), offsets=offs, out=sig, schedule=schedule)
+        assert err, err.message
+        out.append(sig)
+    torch.cuda.synchronize()
+    for k in (1, 2):
+        diff = float(torch.max(torch.abs(out[0] - out[k])).item())
+        assert torch.equal(out[0], out[k]), f"W{W} D{D}: schedule {k} differs by up to {diff:.3e}"
