@@ -480,8 +480,9 @@ def workload_ragged(pkg, torch, args, peak):
     # the grouped launch: team sizes from the tuned separate launches, and a
     # few alternatives; CTA sizes 640 / 512
     cands = []
-    for th64, th32 in {(t64[1] & 1023, t32[1] & 1023), (128, 128), (128, 64), (256, 128), (128, 256),
-                       (256, 64)}:
+    # (team size 0 for the FP32 job: one warp per first letter)
+    for th64, th32 in {(t64[1] & 1023, 0), (128, 0), (256, 0), (t64[1] & 1023, t32[1] & 1023), (128, 128),
+                       (128, 64), (256, 128)}:
         jobs = [pkg.SignatureJob(st64, x64, basis, B, offsets=off_d, out=s64, threads=th64),
                 pkg.SignatureJob(st32, x32, basis, B, offsets=off_d, out=s32, threads=th32)]
         for cta in (640, 512):

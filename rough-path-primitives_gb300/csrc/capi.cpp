@@ -1374,6 +1374,12 @@ int rpp_gb_signature_group(rpp_gb_stream stream, const rpp_gb_signature_job* job
         if (rc) return fail(rc, which + rpp_gb_last_error_string());
         const auto& g = job.plan->geometry;
         int t = job.threads;
+        // FP32 forward-only jobs of an instantiated shape: one warp per first
+        // letter (the kernel of rpp_gb_signature's schedule bit 16), unless
+        // the caller asks for a team size
+        const bool letters = t == 0 && job.dtype == RPP_GB_F32 && job.sig && !job.seed &&
+                             rpp_gb::letter_warps_supported(g.width, g.depth) && 32 * g.width <= cta;
+        if (letters) t = 32 * g.width;
         if (t == 0) {
             // the recorded schedule's (forward) CTA size, else the heuristic
             t = scheduled_threads(schedule_key(job.plan, job.dtype, true, job.sig, job.seed, job.offsets)) & 1023;
@@ -1385,7 +1391,7 @@ int rpp_gb_signature_group(rpp_gb_stream stream, const rpp_gb_signature_job* job
         if (t < 32 || t % 32 != 0 || t < g.depth * g.width || t > cta)
             return fail(RPP_GB_INVALID_ARGUMENT,
                         which + "threads must be a multiple of 32, at least width*depth and at most the CTA size");
-        in[j] = rpp_gb::SignatureJob{g, job.dtype == RPP_GB_F64, t, job.incr,
+        in[j] = rpp_gb::SignatureJob{g, job.dtype == RPP_GB_F64, t, letters, job.incr,
                                      rpp_gb::PathBatch{job.offsets, job.length, job.batch}, job.sig, job.sig_stride,
                                      job.seed, job.seed_stride, job.grad};
     }

@@ -219,6 +219,7 @@ struct SignatureJob {
     Geometry g;
     bool fp64;
     int threads;  // team size (a multiple of 32, at least width * depth)
+    bool letters;  // FP32 forward-only: a team of width warps, one per first letter (threads = 32 width)
     const void* incr;
     PathBatch paths;
     void* sig;

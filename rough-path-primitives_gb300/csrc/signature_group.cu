@@ -1,6 +1,6 @@
 // signature_group.cu -- several signature jobs (different (width, depth)
 // and precisions) in one persistent launch: rpp_gb_signature_group.
-#include "signature_body.cuh"
+#include "signature_letters.cuh"
 
 namespace rpp_gb {
 
@@ -27,6 +27,7 @@ struct GroupJob {
     int32_t depth;
     int32_t fp64;
     int32_t mode;
+    int32_t letters;      // FP32 forward-only: warp-per-letter teams (signature_letters.cuh)
     uint32_t team_threads;
     uint32_t teams;
     uint32_t slice;       // shared-memory bytes of one team (a multiple of 16)
@@ -182,8 +183,48 @@ __device__ __noinline__ void group_team(const SubTeam tm, const uint32_t k) {
     }
 }
 
+// Team k of W warps, one per first letter, on FP32 forward-only paths of the
+// current job (the kernel of signature_fp32.cu, inside the group): each warp
+// works through its slice of the path with __syncwarp only; the team meets on
+// its named barrier to take the next path.
+template <int W, int D>
+__device__ __noinline__ void group_letters(const SubTeam tm, const uint32_t k) {
+    const GroupJob& job = g_job;
+    const uint32_t c = tm.rank() / 32, lane = tm.rank() % 32;
+    float* region = reinterpret_cast<float*>(g_group_smem + static_cast<size_t>(k) * job.slice) +
+                    c * LetterLayout<W, D>::warp_floats;
+    for (;;) {
+        if (tm.rank() == 0) g_task[k] = static_cast<int64_t>(atomicAdd(job.counter, 1u));
+        tm.sync();
+        const int64_t idx = g_task[k];
+        tm.sync();  // every warp has read the slot before the leader rewrites it
+        if (idx >= job.batch) break;
+        const int64_t b = job.order ? job.order[idx] : idx;
+        const int64_t off = job.offsets ? job.offsets[b] : b * job.length;
+        const int64_t len = job.offsets ? job.offsets[b + 1] - off : job.length;
+        letter_path<W, D>(static_cast<const float*>(job.incr), b, off, len, static_cast<float*>(job.sig),
+                          job.sig_stride, region, c, lane);
+    }
+}
+
+__device__ __forceinline__ void group_letters_shape(const SubTeam tm, const uint32_t k) {
+    switch (g_job.width * 100 + g_job.depth) {
+#define RPP_GB_LETTER_CASE(w, d) \
+    case w * 100 + d: group_letters<w, d>(tm, k); break;
+        RPP_GB_LETTER_SHAPES(RPP_GB_LETTER_CASE)
+#undef RPP_GB_LETTER_CASE
+        default: break;
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void group_team_width(const SubTeam tm, const uint32_t k) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (g_job.letters) {
+            group_letters_shape(tm, k);
+            return;
+        }
+    }
     switch (g_job.width) {
         case 2: group_team<T, 2>(tm, k); break;
         case 3: group_team<T, 3>(tm, k); break;
@@ -213,6 +254,18 @@ __global__ void __launch_bounds__(kGroupMaxThreads, 1) k_signature_group(GroupTa
                 group_team_width<float>(tm, k);
         }
         __syncthreads();  // the job, its geometry and the slices are rewritten for the next job
+    }
+}
+
+// Shared memory of one warp-per-letter team (W warps' regions), 0 for a
+// shape without an instantiation.
+size_t letter_slice_bytes(int width, int depth) {
+    switch (width * 100 + depth) {
+#define RPP_GB_LETTER_CASE(w, d) \
+    case w * 100 + d: return (static_cast<size_t>(w) * LetterLayout<w, d>::warp_floats * sizeof(float) + 15) / 16 * 16;
+        RPP_GB_LETTER_SHAPES(RPP_GB_LETTER_CASE)
+#undef RPP_GB_LETTER_CASE
+        default: return 0;
     }
 }
 
@@ -256,7 +309,14 @@ cudaError_t launch_signature_group(const DeviceInfo& dev, cudaStream_t s, const 
         job.mode = kForward | (in.sig ? kTopLevel : 0) | (in.seed && in.grad ? kBackward : 0);
         if ((schedule & kScheduleMergedReverse) && (job.mode & kBackward)) job.mode |= kMergedReverse;
         int mode = job.mode;
-        const size_t slice = in.fp64 ? group_slice<double>(sg, t, mode, optin) : group_slice<float>(sg, t, mode, optin);
+        size_t slice = in.fp64 ? group_slice<double>(sg, t, mode, optin) : group_slice<float>(sg, t, mode, optin);
+        if (in.letters) {
+            if (in.fp64 || job.mode != (kForward | kTopLevel) || t != 32 * in.g.width)
+                return cudaErrorInvalidConfiguration;
+            slice = letter_slice_bytes(in.g.width, in.g.depth);
+            if (slice == 0 || slice > optin) return cudaErrorInvalidConfiguration;
+        }
+        job.letters = in.letters ? 1 : 0;
         if (slice == 0) {
             *refusal = GroupRefusal::StateTooLarge;
             return cudaErrorNotSupported;

@@ -117,6 +117,27 @@ def test_four_jobs_gradient_only_and_team_sizes(orc, bits):
     run_group_and_separate(orc, jobs, schedule=512 | bits)
 
 
+def test_fp32_forward_jobs_take_letter_warps(orc):
+    """FP32 forward-only jobs of an instantiated shape with threads = 0 run with
+    one warp per first letter inside the group; their outputs equal the
+    shared-memory kernel's bit for bit (the same fused multiply-adds), beside
+    an FP64 job in the same launch."""
+    rng = np.random.default_rng(57)
+    jobs = [make_job(rng, 8, 4, 90, torch.float32, ragged=(0, 70), grad=False),
+            make_job(rng, 5, 5, 40, torch.float32, L=19, grad=False),
+            make_job(rng, 8, 4, 60, torch.float64, ragged=(1, 50), grad=False, threads=128)]
+    grouped = [device_args(j) for j in jobs]
+    err = pkg.signature_group(None, [as_job(j, a) for j, a in zip(jobs, grouped)])
+    assert err, err.message
+    torch.cuda.synchronize()
+    for j, a in zip(jobs, grouped):
+        check_oracle(orc, j, a)
+        alone = device_args(j)
+        separate(j, alone, 128)
+        torch.cuda.synchronize()
+        assert torch.equal(a[2], alone[2]), f"W{j['W']} D{j['D']} {j['dtype']}: group differs from a separate call"
+
+
 def test_default_team_sizes(orc):
     """threads = 0: each job takes its shape's heuristic CTA size."""
     rng = np.random.default_rng(56)
