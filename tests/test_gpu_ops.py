@@ -319,3 +319,34 @@ def test_invalid_arguments_are_reported():
     assert not err and err.code == pkg.ErrorCode.InvalidArgument
     assert pkg.ft_mul(st, None, pkg.make_tensor_batch(t, dim, 0, 3), pkg.make_tensor_batch(t, dim, 0, 3),
                       pkg.make_tensor_batch(t, dim, 0, 3), basis, 0)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, TOL_F64), (torch.float32, TOL_F32)])
+@pytest.mark.parametrize("W,D,n", [(4, 4, 1024), (3, 5, 700), (5, 3, 1500)])
+def test_products_large_batches(orc, dtype, tol, W, D, n):
+    """Batches of several tensors per SM (a full wave and more of the product
+    kernel): ft_mul with beta = 1 and beta != 1 and degree ranges, and ft_fma
+    with an addend, against the oracle; odd batch strides put every other row
+    off the 16-byte alignment of the bulk copies."""
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    stride = dim + 3
+    rng = np.random.default_rng(W * 10 + D + n)
+    st = pkg.GB300Strategy(dtype)
+    x, y, z = (rng.uniform(-1, 1, (n, stride)) for _ in range(3))
+    full = (0, D)
+    for rr, beta in [((full, full, full), 1.0), (((1, D), (0, max(0, D - 2)), (1, D)), 0.5)]:
+        out = torch.zeros(n, stride, dtype=dtype, device="cuda")
+        err = pkg.ft_mul(st, None, tb(out, stride, rr[0]), tb(dev(x, dtype), stride, rr[1]),
+                         tb(dev(y, dtype), stride, rr[2]), basis, n, beta)
+        assert err, err.message
+        e = np.zeros((n, stride))
+        orc.ft_mul(W, D, e, x, y, rr, beta)
+        assert_close(host(out)[:, :dim], e[:, :dim], tol, f"ft_mul W{W}D{D} n{n} {rr}")
+    out = torch.zeros(n, stride, dtype=dtype, device="cuda")
+    err = pkg.ft_fma(st, None, tb(out, stride, full), tb(dev(z, dtype), stride, full), tb(dev(x, dtype), stride, full),
+                     tb(dev(y, dtype), stride, full), basis, n, 0.25, 0.75)
+    assert err, err.message
+    e = np.zeros((n, stride))
+    orc.ft_fma(W, D, e, z, x, y, (full, full, full, full), 0.25, 0.75)
+    assert_close(host(out)[:, :dim], e[:, :dim], tol, f"ft_fma W{W}D{D} n{n}")
