@@ -531,7 +531,7 @@ def workload_ragged_fp32(pkg, torch, args, peak):
         err, sched, _ = pkg.signature_tune(st32, None, x32, basis, B, offsets=off_d, out=s32)
         err.raise_if_failed()
     ms = 1e3 * _time_launches(torch, lambda: pkg.signature(st32, None, x32, basis, B, offsets=off_d, out=s32,
-                                                           schedule=sched),
+                                                           schedule=sched).raise_if_failed(),
                               args.steps, args.warmup, torch.cuda.current_stream())
     flops = 2.0 * int(offsets[-1]) * step_fma(W, D)
     _line("uneven-length signatures paths/sec (W8 D4, L~U[16,2048], FP32 forward)", B / (ms / 1e3), "paths/s", ms,
@@ -657,7 +657,7 @@ def workload_fwd_bwd(pkg, torch, args, peak, W, D, B, L, name):
         err.raise_if_failed()
     ms = 1e3 * _time_launches(
         torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad,
-                                     schedule=args.schedule),
+                                     schedule=args.schedule).raise_if_failed(),
         args.steps, args.warmup, torch.cuda.current_stream())
     _line(f"signature fwd+bwd paths/sec (W{W} D{D} L{L} FP64)", B / (ms / 1e3), "paths/s", ms, "f64",
           {"workload": name, "batch": B, "length": L, "schedule": threads, "threads_per_cta": threads & 1023,

@@ -349,7 +349,7 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         return rc;
     static const int sizes[] = {128, 192, 256, 320, 384, 512};
     static const int caps[] = {0, 3, 2};
-    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 8 + 32];
+    int candidates[sizeof(sizes) / sizeof(sizes[0]) * 8 + 64];
     int ncand = 0;
     for (int c : caps)
         for (int t : sizes) candidates[ncand++] = t | (c << 10);
@@ -382,7 +382,10 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
             if (P <= geo.width && geo.width % P == 0)
                 for (int t : {256, 512})
                     for (int top : {0, rpp_gb::kScheduleForwardTopGlobal})
-                        candidates[ncand++] = t | top | ((P - 1) << rpp_gb::kScheduleClusterShift);
+                        for (int cot : {0, rpp_gb::kScheduleCotangentGlobal}) {
+                            if (cot && !(seed && grad)) continue;
+                            candidates[ncand++] = t | top | cot | ((P - 1) << rpp_gb::kScheduleClusterShift);
+                        }
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return fail(RPP_GB_OUT_OF_RESOURCES, "cudaEventCreate failed");

@@ -159,7 +159,10 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
         // kScheduleForwardTopGlobal: the top level in the signature / seed
         // rows (less shared memory per CTA, more clusters resident)
         const int t = (schedule & 1023) ? (schedule & 1023) : threads_for(sg.g.pw[sg.g.depth] / cluster);
-        const int m = (schedule & kScheduleForwardTopGlobal) ? (mode | kTopGlobal) : mode;
+        // kScheduleCotangentGlobal: the cotangent level and chains in a
+        // per-CTA global workspace (less shared memory per CTA again)
+        int m = (schedule & kScheduleForwardTopGlobal) ? (mode | kTopGlobal) : mode;
+        if (bwd && (schedule & kScheduleCotangentGlobal)) m |= kCotGlobal;
         return launch_signature_split<T>(sg.g, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, m,
                                          std::max(t, (sg.g.depth * sg.g.width + 31) / 32 * 32), cluster);
     }

@@ -109,16 +109,20 @@ __device__ __forceinline__ void run_path_split(const CtaTeam& tm, const SigGeome
 // it to the cluster's CTAs through distributed shared memory, in a slot of
 // the iteration's parity (a CTA reads slot i mod 2 before arriving on the
 // barrier that precedes the next write of that slot).
-template <typename T, int WT>
+// COT: the cotangent level and chains in this CTA's slice of the global
+// workspace `gws` (kCotGlobal, L2-resident), the state and forward chains in
+// shared memory.
+template <typename T, int WT, bool COT>
 __global__ void __launch_bounds__(kResidentMaxThreads, 2) k_signature_split(SigGeometry sg, LevelStarts full,
                                                                            const T* __restrict__ incr, PathBatch paths,
                                                                            T* sig, int64_t sig_stride, const T* seed,
-                                                                           int64_t seed_stride, T* grad, int mode) {
+                                                                           int64_t seed_stride, T* grad, int mode,
+                                                                           T* gws, int64_t gws_stride) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int64_t s_next[2];
     const CtaTeam tm;
     bool vec4 = false;
-    SigShared<T> sh = place_arrays<T, WT, false>(tm, sg, mode, static_cast<T*>(nullptr), 0, smem_raw, vec4);
+    SigShared<T> sh = place_arrays<T, WT, COT>(tm, sg, mode, gws, gws_stride, smem_raw, vec4);
     uint32_t P;
     asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(P));
     const uint32_t rank = cluster_rank();
@@ -162,6 +166,11 @@ SigGeometry sliced_geometry(const Geometry& g, int P) {
     return make_sig_geometry(s);
 }
 
+template <typename T, int WT, bool COT>
+cudaError_t launch_split_kernel(const SigGeometry& sg, const LevelStarts& full, const DeviceInfo& dev,
+                                cudaStream_t s, const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
+                                const T* seed, int64_t seed_stride, T* grad, int mode, int threads, int P);
+
 template <typename T, int WT>
 cudaError_t launch_split_width(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const T* incr,
                                PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
@@ -169,18 +178,31 @@ cudaError_t launch_split_width(const Geometry& g, const DeviceInfo& dev, cudaStr
     const SigGeometry sg = sliced_geometry(g, P);
     LevelStarts full{};
     for (int j = 0; j <= g.depth + 1; ++j) full.db[j] = g.db[j];
-    constexpr auto kernel = k_signature_split<T, WT>;
+    const bool cot = (mode & kCotGlobal) && (mode & kBackward);
+    if (cot) return launch_split_kernel<T, WT, true>(sg, full, dev, s, incr, paths, sig, sig_stride, seed, seed_stride,
+                                                     grad, mode, threads, P);
+    return launch_split_kernel<T, WT, false>(sg, full, dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad,
+                                             mode & ~kCotGlobal, threads, P);
+}
+
+template <typename T, int WT, bool COT>
+cudaError_t launch_split_kernel(const SigGeometry& sg, const LevelStarts& full, const DeviceInfo& dev,
+                                cudaStream_t s, const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
+                                const T* seed, int64_t seed_stride, T* grad, int mode, int threads, int P) {
+    const Geometry& g = sg.g;
+    constexpr auto kernel = k_signature_split<T, WT, COT>;
     cudaError_t err = allow_large_smem<kernel>(dev);
     if (err != cudaSuccess) return err;
     cudaFuncAttributes attr{};
     if ((err = cudaFuncGetAttributes(&attr, kernel)) != cudaSuccess) return err;
     const size_t optin = static_cast<size_t>(dev.max_smem_optin) - attr.sharedSizeBytes;
-    const bool bwd = mode & kBackward;
+    // with COT the cotangent arrays are not in shared memory
+    const bool bwd_smem = (mode & kBackward) && !COT;
     const size_t slots = 2 * static_cast<size_t>(P) * g.width * sizeof(T);
-    size_t smem = sig_smem_bytes<T>(sg, threads, bwd, true, mode & kTopGlobal) + slots;
+    size_t smem = sig_smem_bytes<T>(sg, threads, bwd_smem, true, mode & kTopGlobal) + slots;
     if (smem > optin && !(mode & kTopGlobal)) {
         mode |= kTopGlobal;
-        smem = sig_smem_bytes<T>(sg, threads, bwd, true, true) + slots;
+        smem = sig_smem_bytes<T>(sg, threads, bwd_smem, true, true) + slots;
     }
     if (smem > optin) return cudaErrorInvalidConfiguration;
     cudaLaunchConfig_t cfg{};
@@ -200,7 +222,21 @@ cudaError_t launch_split_width(const Geometry& g, const DeviceInfo& dev, cudaStr
     if (clusters < 1) return cudaErrorInvalidConfiguration;
     const int64_t n = std::max<int64_t>(1, std::min<int64_t>(paths.batch, clusters));
     cfg.gridDim = dim3(static_cast<unsigned>(n * P));
-    return cudaLaunchKernelEx(&cfg, kernel, sg, full, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
+    if constexpr (!COT) {
+        return cudaLaunchKernelEx(&cfg, kernel, sg, full, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode,
+                                  static_cast<T*>(nullptr), int64_t{0});
+    } else {
+        // the cotangent level (below the top) and chains of each CTA, in a
+        // stream-ordered workspace released after the launch
+        const int64_t stride = static_cast<int64_t>((sg.g.db[sg.g.depth] + sg.chain_total + 31) / 32 * 32);
+        T* ws = nullptr;
+        err = cudaMallocAsync(reinterpret_cast<void**>(&ws), static_cast<size_t>(n * P) * stride * sizeof(T), s);
+        if (err != cudaSuccess) return err;
+        err = cudaLaunchKernelEx(&cfg, kernel, sg, full, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode,
+                                 ws, stride);
+        cudaError_t ferr = cudaFreeAsync(ws, s);
+        return err != cudaSuccess ? err : ferr;
+    }
 }
 
 }  // namespace
@@ -210,7 +246,7 @@ cudaError_t launch_signature_split(const Geometry& g, const DeviceInfo& dev, cud
                                    PathBatch paths, T* sig, int64_t sig_stride, const T* seed, int64_t seed_stride,
                                    T* grad, int mode, int threads, int P) {
     if (P < 2 || P > 8 || g.width % P != 0 || g.depth < 2) return cudaErrorInvalidConfiguration;
-    if (mode & (kLoadFinal | kCotGlobal | kMergedReverse)) return cudaErrorInvalidConfiguration;
+    if (mode & (kLoadFinal | kMergedReverse)) return cudaErrorInvalidConfiguration;
     if (threads % 32 != 0 || threads > kResidentMaxThreads || threads < g.depth * g.width)
         return cudaErrorInvalidConfiguration;
     switch (g.width) {

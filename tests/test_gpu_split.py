@@ -53,7 +53,10 @@ def check(orc, W, D, incr, offsets, ell, sig, grad, tol, what):
     (2, 12, 2, 3, 10, 256), (2, 12, 2, 2, 7, 512), (4, 5, 2, 5, 12, 256), (4, 5, 4, 5, 12, 256),
     (3, 6, 3, 4, 9, 256), (8, 4, 8, 4, 8, 256), (8, 4, 2, 4, 8, 512),
     # bit 15: the top level in the signature and seed rows
-    (6, 6, 6, 3, 6, 256 | (1 << 15)), (4, 5, 4, 5, 12, 128 | (1 << 15))])
+    (6, 6, 6, 3, 6, 256 | (1 << 15)), (4, 5, 4, 5, 12, 128 | (1 << 15)),
+    # bit 26: the cotangent level and chains in a global workspace
+    (2, 12, 2, 3, 10, 256 | (1 << 26)), (2, 12, 2, 2, 7, 512 | (1 << 15) | (1 << 26)),
+    (6, 6, 3, 3, 6, 512 | (1 << 26)), (3, 6, 3, 4, 9, 128 | (1 << 26))])
 def test_forward_and_reverse_fp64(orc, W, D, P, B, L, threads):
     rng = np.random.default_rng(W * 1000 + D * 10 + P)
     incr = rng.normal(0, 1 / np.sqrt(L), (B * L, W))
@@ -80,14 +83,14 @@ def test_gradient_only(orc):
     check(orc, W, D, incr, np.arange(B + 1) * L, ell, None, grad, TOL_F64, "W6 D6 P3 gradient only")
 
 
-@pytest.mark.parametrize("W,D,P", [(6, 5, 3), (2, 10, 2), (4, 4, 4)])
-def test_ragged_with_empty_and_unit_paths(orc, W, D, P):
+@pytest.mark.parametrize("W,D,P,cot", [(6, 5, 3, 0), (2, 10, 2, 0), (4, 4, 4, 0), (2, 10, 2, 1 << 26)])
+def test_ragged_with_empty_and_unit_paths(orc, W, D, P, cot):
     rng = np.random.default_rng(100 + W * D + P)
     lengths = np.array([0, 1, 13, 2, 0, 9, 1, 21, 5])
     offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
     incr = rng.normal(0, 0.3, (int(offsets[-1]), W))
     ell = rng.uniform(-1, 1, (len(lengths), O.tensor_dim(W, D)))
-    sig, grad = run(W, D, incr, split(P, 256), offsets=offsets, ell=ell)
+    sig, grad = run(W, D, incr, split(P, 256) | cot, offsets=offsets, ell=ell)
     check(orc, W, D, incr, offsets, ell, sig, grad, TOL_F64, f"ragged W{W} D{D} P{P}")
 
 
