@@ -279,7 +279,13 @@ struct SigLaunches {
     int schedule[2] = {0, 0};
 };
 
-SigLaunches plan_launches(bool forward, bool has_sig, bool has_seed, bool has_grad, int threads) {
+// `letters`: the call is FP32 of a shape the warp-per-letter forward kernel
+// is instantiated for; its forward-only launches then take that kernel (bit
+// 16 of their own schedule word) unless a schedule fixes the CTA size: the
+// forward launch of the two-launch form, and forward-only calls without a
+// recorded schedule.  Its results equal the shared-memory kernel's bit for bit.
+SigLaunches plan_launches(bool forward, bool has_sig, bool has_seed, bool has_grad, int threads,
+                          bool letters = false) {
     SigLaunches l;
     const bool split = forward && has_sig && has_seed && has_grad && threads > 0 && (threads & kScheduleSplit);
     if (split) {
@@ -289,7 +295,7 @@ SigLaunches plan_launches(bool forward, bool has_sig, bool has_seed, bool has_gr
         const int fwd = threads & ((1 << 14) - 1);  // CTA size and cap
         l.count = 2;
         l.mode[0] = kForward | kTopLevel | (fwd_top_global ? kTopGlobal : 0);
-        l.schedule[0] = fwd;
+        l.schedule[0] = (letters && !fwd_top_global) ? (32 | kScheduleLetterWarps) : fwd;
         l.mode[1] = kBackward | kLoadFinal | kTopGlobal;
         l.schedule[1] = (rev > 0 ? (fwd & ~1023) | rev : fwd) | cot;
         return l;
@@ -305,7 +311,7 @@ SigLaunches plan_launches(bool forward, bool has_sig, bool has_seed, bool has_gr
     }
     l.count = 1;
     l.mode[0] = mode;
-    l.schedule[0] = threads;
+    l.schedule[0] = (letters && threads == 0 && mode == (kForward | kTopLevel)) ? (32 | kScheduleLetterWarps) : threads;
     return l;
 }
 
@@ -332,7 +338,8 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
                              T* grad, bool forward, int threads) {
     if (paths.batch <= 0) return cudaSuccess;
     const SigGeometry sg = make_sig_geometry(g);
-    const SigLaunches launches = plan_launches(forward, sig != nullptr, seed != nullptr, grad != nullptr, threads);
+    const SigLaunches launches = plan_launches(forward, sig != nullptr, seed != nullptr, grad != nullptr, threads,
+                                               std::is_same<T, float>::value && letter_warps_supported(g.width, g.depth));
     // Ragged batches: order the paths longest first and hand them out through
     // a work counter (stream-ordered scratch, released after the launch).
     void* scratch = nullptr;
@@ -414,7 +421,8 @@ cudaError_t launch_signature_static_scratch(const Geometry& g, const DeviceInfo&
     // which is an allocation: that launch runs with its cotangent arrays in
     // shared memory instead (same results).
     if (threads > 0) threads &= ~kScheduleCotangentGlobal;
-    const SigLaunches launches = plan_launches(true, sig != nullptr, seed != nullptr, grad != nullptr, threads);
+    const SigLaunches launches = plan_launches(true, sig != nullptr, seed != nullptr, grad != nullptr, threads,
+                                               std::is_same<T, float>::value && letter_warps_supported(g.width, g.depth));
     // Only the shared-memory kernel allocates nothing: every launch of the
     // call must take it, checked before anything is launched.
     for (int i = 0; i < launches.count; ++i) {
