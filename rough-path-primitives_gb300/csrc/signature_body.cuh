@@ -747,12 +747,30 @@ __device__ __forceinline__ void backward_step(const Team& tm, const SigGeometry&
                         T* gout = chain(sg, sh.Tb, n, j - 1);
                         T x[WT];
                         load_row(x, xc + (n - j + 2) * WT);
-                        for (; r < wjm1; r += tm.size()) {
+                        // two rows per iteration, both rows' loads issued
+                        // before either sum (the top stage's rows come from
+                        // L2 when the seed's top level stays in global memory)
+                        const uint32_t bd = tm.size();
+                        for (; r + bd < wjm1; r += 2 * bd) {
+                            T g0[WT], g1[WT];
+                            load_row(g0, gin + r * WT);
+                            load_row(g1, gin + (r + bd) * WT);
+                            T acc0 = T(0), acc1 = T(0);
+#pragma unroll
+                            for (int a = 0; a < WT; ++a) {
+                                acc0 = fma(g0[a], x[a], acc0);
+                                acc1 = fma(g1[a], x[a], acc1);
+                            }
+                            gout[r] = acc0;
+                            gout[r + bd] = acc1;
+                        }
+                        if (r < wjm1) {
                             const T* row = gin + r * WT;
                             T acc = T(0);
 #pragma unroll
                             for (int a = 0; a < WT; ++a) acc = fma(row[a], x[a], acc);
                             gout[r] = acc;
+                            r += bd;
                         }
                     }
                     r -= wjm1;
