@@ -601,7 +601,7 @@ def workload_fp32(pkg, torch, args, peak):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    W, D, B, L = WIDTH, DEPTH, BATCH, LENGTH
+    W, D, B, L = WIDTH, DEPTH, args.batch, LENGTH
     out = ctypes.c_double(0)
     peak32 = out.value if pkg.library().rpp_gb_fma_peak(0, 0, ctypes.byref(out)) == 0 else None
     basis = pkg.TensorBasis(W, D)
@@ -617,19 +617,24 @@ def workload_fp32(pkg, torch, args, peak):
     lines = []
     for what, kw, fma in (("fwd+bwd", {"seed": ell, "grad": grad}, 4 * step_fma(W, D)),
                           ("forward", {}, step_fma(W, D))):
-        err, threads, _ = pkg.signature_tune(st, None, incr, basis, B, length=L, out=sig, **kw)
-        err.raise_if_failed()
-        ms = 1e3 * _time_launches(torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, **kw),
-                                  args.steps, args.warmup, cur)
+        if args.schedule is not None:  # a pinned schedule (profiling captures)
+            threads = args.schedule
+            kw = dict(kw, schedule=threads)
+        else:
+            err, threads, _ = pkg.signature_tune(st, None, incr, basis, B, length=L, out=sig, **kw)
+            err.raise_if_failed()
+        ms = 1e3 * _time_launches(
+            torch, lambda: pkg.signature(st, None, incr, basis, B, length=L, out=sig, **kw).raise_if_failed(),
+            args.steps, args.warmup, cur)
         flops = 2.0 * fma * L * B
         n = 3
         esig, egrad = O.Oracle().signature(W, D, incr64[:n * L].cpu().numpy(), np.arange(n + 1) * L,
-                                           ell=ell64[:n].cpu().numpy() if kw else None)
+                                           ell=ell64[:n].cpu().numpy() if "seed" in kw else None)
         err_sig = float(np.max(np.abs(sig[:n].double().cpu().numpy() - esig) / np.maximum(1, np.abs(esig))))
         extra = {"fp32_tflops": flops / (ms / 1e3) / 1e12, "fp32_peak_tflops": peak32,
                  "fp32_peak_frac": flops / (ms / 1e3) / 1e12 / peak32 if peak32 else None,
                  "max_rel_err_sig_vs_fp64_oracle": err_sig}
-        if kw:
+        if "seed" in kw:
             gg = grad[:n * L].double().cpu().numpy()
             extra["max_scaled_err_grad_vs_fp64_oracle"] = float(np.max(np.abs(gg - egrad)) /
                                                                 max(1.0, float(np.max(np.abs(egrad)))))

@@ -370,9 +370,11 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
                     candidates[ncand++] = t | rpp_gb::kScheduleSplit | rpp_gb::kScheduleForwardTopGlobal |
                                           rpp_gb::kScheduleCotangentGlobal | (rev << rpp_gb::kScheduleReverseShift);
         }
-    // forward-only FP32: the kernel with one warp per first letter
-    if (std::is_same<T, float>::value && sig && !seed &&
-        rpp_gb::letter_warps_supported(plan->geometry.width, plan->geometry.depth))
+    // FP32: the kernels with one warp per first letter (forward-only, and
+    // forward + reverse)
+    if (std::is_same<T, float>::value &&
+        ((sig && !seed && rpp_gb::letter_warps_supported(plan->geometry.width, plan->geometry.depth)) ||
+         (seed && rpp_gb::letter_reverse_supported(plan->geometry.width, plan->geometry.depth))))
         candidates[ncand++] = 32 | rpp_gb::kScheduleLetterWarps;
     // a state split over a cluster of P CTAs by first letter (P divides the
     // width), for states whose tensor alone exceeds 48 KB
@@ -452,7 +454,8 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
         int base[3];
         for (int k = 0; k < 3; ++k) base[k] = top[k].second;
         for (int k = 0; k < 3; ++k)
-            if (base[k] != 0 && ((base[k] >> rpp_gb::kScheduleClusterShift) & 7) == 0)
+            if (base[k] != 0 && ((base[k] >> rpp_gb::kScheduleClusterShift) & 7) == 0 &&
+                !((base[k] & rpp_gb::kScheduleLetterWarps) && !(base[k] & rpp_gb::kScheduleSplit)))
                 try_candidate(base[k] | rpp_gb::kScheduleMergedReverse);
     }
     // Near-ties are decided by noise in a single timing: time the three

@@ -193,13 +193,20 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
                              const T* incr, PathBatch paths, T* sig, int64_t sig_stride,
                              const T* seed, int64_t seed_stride, T* grad, bool forward, int threads);
 
-// kScheduleLetterWarps (bit 16 of a forward-only FP32 call's schedule, where
-// bits 16-25 have no other use): the FP32 forward kernel with one warp per
-// first letter and compile-time (width, depth) (signature_fp32.cu).
+// kScheduleLetterWarps (bit 16 of an FP32 call's schedule without
+// kScheduleSplit, where bits 16-25 have no other use): the FP32 kernels with
+// one warp per first letter and compile-time (width, depth)
+// (signature_fp32.cu) -- the forward-only kernel, and for calls with a
+// reverse pass (depth >= 3) the forward + reverse kernel.
 constexpr int kScheduleLetterWarps = 1 << 16;
 bool letter_warps_supported(int width, int depth);
+bool letter_reverse_supported(int width, int depth);
 cudaError_t launch_signature_letters(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const float* incr,
                                      PathBatch paths, float* sig, int64_t sig_stride);
+// `mode`: kForward | kBackward [| kTopLevel], or kBackward | kLoadFinal.
+cudaError_t launch_signature_letters_rev(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const float* incr,
+                                         PathBatch paths, float* sig, int64_t sig_stride, const float* seed,
+                                         int64_t seed_stride, float* grad, int mode);
 
 // Split-state launch (kScheduleClusterShift): `mode` as launch_width's, CTA
 // size `threads`, `P` CTAs per cluster.

@@ -150,9 +150,14 @@ cudaError_t launch_width(const SigGeometry& sg, const DeviceInfo& dev, cudaStrea
                          int mode, int schedule) {
     const bool bwd = mode & kBackward;
     if constexpr (std::is_same<T, float>::value) {
-        // forward-only FP32 with one warp per first letter (signature_fp32.cu)
-        if (schedule > 0 && (schedule & kScheduleLetterWarps) && mode == (kForward | kTopLevel))
-            return launch_signature_letters(sg.g, dev, s, incr, paths, sig, sig_stride);
+        // FP32 with one warp per first letter (signature_fp32.cu)
+        if (schedule > 0 && (schedule & kScheduleLetterWarps) && !(schedule & kScheduleSplit)) {
+            if (mode == (kForward | kTopLevel))
+                return launch_signature_letters(sg.g, dev, s, incr, paths, sig, sig_stride);
+            if (bwd && letter_reverse_supported(sg.g.width, sg.g.depth))
+                return launch_signature_letters_rev(sg.g, dev, s, incr, paths, sig, sig_stride, seed, seed_stride,
+                                                    grad, mode);
+        }
     }
     const int cluster = schedule > 0 ? ((schedule >> kScheduleClusterShift) & 7) + 1 : 1;
     if (cluster >= 2) {  // the state split over a cluster of CTAs (signature_split.cu)
@@ -284,8 +289,10 @@ struct SigLaunches {
 // 16 of their own schedule word) unless a schedule fixes the CTA size: the
 // forward launch of the two-launch form, and forward-only calls without a
 // recorded schedule.  Its results equal the shared-memory kernel's bit for bit.
+// `letters_rev`: the shape has the warp-per-letter reverse kernel too, which
+// calls with a reverse pass and no recorded schedule then take.
 SigLaunches plan_launches(bool forward, bool has_sig, bool has_seed, bool has_grad, int threads,
-                          bool letters = false) {
+                          bool letters = false, bool letters_rev = false) {
     SigLaunches l;
     const bool split = forward && has_sig && has_seed && has_grad && threads > 0 && (threads & kScheduleSplit);
     if (split) {
@@ -311,7 +318,9 @@ SigLaunches plan_launches(bool forward, bool has_sig, bool has_seed, bool has_gr
     }
     l.count = 1;
     l.mode[0] = mode;
-    l.schedule[0] = (letters && threads == 0 && mode == (kForward | kTopLevel)) ? (32 | kScheduleLetterWarps) : threads;
+    const bool letter_kernel = threads == 0 && ((letters && mode == (kForward | kTopLevel)) ||
+                                                (letters_rev && (mode & kBackward)));
+    l.schedule[0] = letter_kernel ? (32 | kScheduleLetterWarps) : threads;
     return l;
 }
 
@@ -338,8 +347,10 @@ cudaError_t launch_signature(const Geometry& g, const DeviceInfo& dev, cudaStrea
                              T* grad, bool forward, int threads) {
     if (paths.batch <= 0) return cudaSuccess;
     const SigGeometry sg = make_sig_geometry(g);
+    constexpr bool fp32 = std::is_same<T, float>::value;
     const SigLaunches launches = plan_launches(forward, sig != nullptr, seed != nullptr, grad != nullptr, threads,
-                                               std::is_same<T, float>::value && letter_warps_supported(g.width, g.depth));
+                                               fp32 && letter_warps_supported(g.width, g.depth),
+                                               fp32 && letter_reverse_supported(g.width, g.depth));
     // Ragged batches: order the paths longest first and hand them out through
     // a work counter (stream-ordered scratch, released after the launch).
     void* scratch = nullptr;
@@ -421,8 +432,10 @@ cudaError_t launch_signature_static_scratch(const Geometry& g, const DeviceInfo&
     // which is an allocation: that launch runs with its cotangent arrays in
     // shared memory instead (same results).
     if (threads > 0) threads &= ~kScheduleCotangentGlobal;
+    constexpr bool fp32 = std::is_same<T, float>::value;
     const SigLaunches launches = plan_launches(true, sig != nullptr, seed != nullptr, grad != nullptr, threads,
-                                               std::is_same<T, float>::value && letter_warps_supported(g.width, g.depth));
+                                               fp32 && letter_warps_supported(g.width, g.depth),
+                                               fp32 && letter_reverse_supported(g.width, g.depth));
     // Only the shared-memory kernel allocates nothing: every launch of the
     // call must take it, checked before anything is launched.
     for (int i = 0; i < launches.count; ++i) {

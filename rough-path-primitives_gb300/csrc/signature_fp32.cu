@@ -1,6 +1,7 @@
-// signature_fp32.cu -- FP32 forward signatures with one warp per first letter
-// (schedule bit 16 on forward-only calls, kScheduleLetterWarps): the kernel
-// and its launch; the step and per-path code are in signature_letters.cuh.
+// signature_fp32.cu -- FP32 signatures with one warp per first letter
+// (schedule bit 16, kScheduleLetterWarps): the forward-only kernel, the
+// forward + reverse kernel, and their launches; the steps and per-path code
+// are in signature_letters.cuh.
 #include "signature_letters.cuh"
 
 namespace rpp_gb {
@@ -44,6 +45,74 @@ __global__ void __launch_bounds__(W * 32, letter_min_blocks(W, D)) k_signature_l
     }
 }
 
+// Registers for the reverse kernel: 24 warps per SM (about 85 registers a
+// thread: the seed's top rows, levels D-1 of S and G, the letter sums and the
+// increment ring).
+constexpr int letter_rev_min_blocks(int W) { return 768 / (W * 32) > 0 ? 768 / (W * 32) : 1; }
+
+// Forward + reverse (or reverse from the final signature) with one warp per
+// first letter: a CTA of W warps runs one path at a time.
+template <int W, int D>
+__global__ void __launch_bounds__(W * 32, letter_rev_min_blocks(W))
+    k_signature_letters_rev(const float* __restrict__ incr, PathBatch paths, float* sig, int64_t sig_stride,
+                            const float* __restrict__ seed, int64_t seed_stride, float* grad, int mode) {
+    using Rev = LetterRevLayout<W, D>;
+    extern __shared__ __align__(16) float sm_letters[];
+    __shared__ int64_t s_next;
+    const uint32_t c = threadIdx.x / 32;
+    const uint32_t lane = threadIdx.x % 32;
+    float* region = sm_letters + c * Rev::warp_floats;
+    float* pbuf = sm_letters + W * Rev::warp_floats;
+    int64_t slot = blockIdx.x;
+    if (paths.counter) {
+        if (threadIdx.x == 0) s_next = static_cast<int64_t>(atomicAdd(paths.counter, 1u));
+        __syncthreads();
+        slot = s_next;
+        __syncthreads();
+    }
+    while (slot < paths.batch) {
+        const int64_t b = paths.order ? paths.order[slot] : slot;
+        const int64_t off = paths.offsets ? paths.offsets[b] : b * paths.length;
+        const int64_t len = paths.offsets ? paths.offsets[b + 1] - off : paths.length;
+        letter_fwd_bwd<W, D>(incr, b, off, len, sig, sig_stride, seed, seed_stride, grad, mode, region, pbuf, c,
+                             lane);
+        __syncthreads();  // the last block's partials are read before the next path writes pbuf
+        if (paths.counter) {
+            if (threadIdx.x == 0) s_next = static_cast<int64_t>(atomicAdd(paths.counter, 1u));
+            __syncthreads();
+            slot = s_next;
+            __syncthreads();
+        } else {
+            slot += gridDim.x;
+        }
+    }
+}
+
+template <int W, int D>
+cudaError_t launch_letters_rev_shape(const DeviceInfo& dev, cudaStream_t s, const float* incr, PathBatch paths,
+                                     float* sig, int64_t sig_stride, const float* seed, int64_t seed_stride,
+                                     float* grad, int mode) {
+    using Rev = LetterRevLayout<W, D>;
+    constexpr auto kernel = k_signature_letters_rev<W, D>;
+    const size_t smem = (static_cast<size_t>(W) * Rev::warp_floats + Rev::pbuf_floats) * sizeof(float);
+    dim3 grid;
+    cudaError_t err = batch_grid(kernel, dev, W * 32, smem, paths.batch, grid);
+    if (err != cudaSuccess) return err;
+    kernel<<<grid, W * 32, smem, s>>>(incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
+    return cudaGetLastError();
+}
+
+// The reverse kernel needs level D-1 in registers (D >= 3).
+template <int W, int D>
+cudaError_t launch_letters_rev_if(const DeviceInfo& dev, cudaStream_t s, const float* incr, PathBatch paths,
+                                  float* sig, int64_t sig_stride, const float* seed, int64_t seed_stride, float* grad,
+                                  int mode) {
+    if constexpr (D >= 3)
+        return launch_letters_rev_shape<W, D>(dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
+    else
+        return cudaErrorInvalidConfiguration;
+}
+
 template <int W, int D>
 cudaError_t launch_letters_shape(const DeviceInfo& dev, cudaStream_t s, const float* incr, PathBatch paths,
                                  float* sig, int64_t sig_stride) {
@@ -65,6 +134,20 @@ bool letter_warps_supported(int width, int depth) {
         RPP_GB_LETTER_SHAPES(RPP_GB_LETTER_CASE)
 #undef RPP_GB_LETTER_CASE
         default: return false;
+    }
+}
+
+bool letter_reverse_supported(int width, int depth) { return depth >= 3 && letter_warps_supported(width, depth); }
+
+cudaError_t launch_signature_letters_rev(const Geometry& g, const DeviceInfo& dev, cudaStream_t s, const float* incr,
+                                         PathBatch paths, float* sig, int64_t sig_stride, const float* seed,
+                                         int64_t seed_stride, float* grad, int mode) {
+    switch (g.width * 100 + g.depth) {
+#define RPP_GB_LETTER_CASE(w, d) \
+    case w * 100 + d: return launch_letters_rev_if<w, d>(dev, s, incr, paths, sig, sig_stride, seed, seed_stride, grad, mode);
+        RPP_GB_LETTER_SHAPES(RPP_GB_LETTER_CASE)
+#undef RPP_GB_LETTER_CASE
+        default: return cudaErrorInvalidConfiguration;
     }
 }
 

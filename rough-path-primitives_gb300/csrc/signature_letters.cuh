@@ -98,11 +98,13 @@ constexpr int lower_per_lane() {
 // index arithmetic.  All lanes read the old levels before any lane writes the
 // new ones (one __syncwarp between); the caller's __syncwarp after refreshing
 // the increment orders the writes before the next step's reads.
+// `with_top` false: the top rows are left alone (a gradient-only call needs
+// levels 1..D-1 only).
 template <int W, int D>
 __device__ __forceinline__ void letter_step(float* S, const float* x,
                                             float (&top)[LetterLayout<W, D>::rows_per_lane][W],
                                             float (&sd)[LetterLayout<W, D>::rows_per_lane], uint32_t c,
-                                            uint32_t lane) {
+                                            uint32_t lane, bool with_top = true) {
     using Lay = LetterLayout<W, D>;
     constexpr int R = Lay::rows_per_lane;
     constexpr int NS = Lay::smem_levels;  // levels in shared memory: 1..NS
@@ -174,8 +176,10 @@ __device__ __forceinline__ void letter_step(float* S, const float* x,
                 accd = fmaf(accd, __fmul_rn(xa, 0.5f), sd[r]);  // T^D_{D-1}: old S_{D-1}
                 sd[r] = fmaf(accm, xa, sd[r]);       // new S_{D-1} = T^{D-1}_{D-1}
             }
+            if (with_top) {
 #pragma unroll
-            for (int a = 0; a < W; ++a) top[r][a] = fmaf(accd, x1[a], top[r][a]);
+                for (int a = 0; a < W; ++a) top[r][a] = fmaf(accd, x1[a], top[r][a]);
+            }
         }
     }
     __syncwarp();  // every lane has read the old levels
@@ -193,27 +197,24 @@ __device__ __forceinline__ void letter_step(float* S, const float* x,
     }
 }
 
-// One path b with increments [off, off + len) by warp c of the path's W
-// warps (its first-letter slice), into the signature row sig + b*sig_stride.
-// `region` is the warp's shared memory (LetterLayout::warp_floats floats:
-// two increment buffers, then the levels kept in shared memory).  Warps
-// never wait on each other; ends with __syncwarp.
+// The forward pass of one path with increments [off, off + len) by warp c of
+// the path's W warps (its first-letter slice): leaves levels 1..smem_levels
+// of the slice in S, level D-1 in sd and, with `with_top`, the top rows in
+// `top`.  `xcb` holds the two increment buffers (2 xcs floats).  Warps never
+// wait on each other; ends with __syncwarp.
 template <int W, int D>
-__device__ __forceinline__ void letter_path(const float* __restrict__ incr, int64_t b, int64_t off, int64_t len,
-                                            float* sig, int64_t sig_stride, float* region, uint32_t c,
-                                            uint32_t lane) {
+__device__ __forceinline__ void letter_forward(const float* __restrict__ incr, int64_t off, int64_t len, float* xcb,
+                                               float* S, float (&top)[LetterLayout<W, D>::rows_per_lane][W],
+                                               float (&sd)[LetterLayout<W, D>::rows_per_lane], uint32_t c,
+                                               uint32_t lane, bool with_top) {
     using Lay = LetterLayout<W, D>;
     static_assert(D >= 2 && W <= 32, "one letter per lane");
     static_assert(LetterLayout<W, D>::rows_per_lane * W <= 32, "at most 32 registers of top-level rows");
     constexpr int R = Lay::rows_per_lane;
     constexpr int PF = 8;  // increments prefetched ahead
-    float* xcb = region;             // two increment buffers
-    float* S = xcb + 2 * Lay::xcs;   // levels 1..smem_levels
     const bool xlane = lane < static_cast<uint32_t>(W);  // lane a < W holds letter a
     const float* xin = incr + off * W;
     for (uint32_t i = lane; i < Lay::s_size; i += 32) S[i] = 0.0f;
-    float top[R][W];
-    float sd[R];  // this lane's coefficients of level D-1 (when in registers)
 #pragma unroll
     for (int i = 0; i < R; ++i) {
         sd[i] = 0.0f;
@@ -236,14 +237,22 @@ __device__ __forceinline__ void letter_path(const float* __restrict__ incr, int6
             // slot q has been consumed (x_k is in the increment buffer):
             // refill it with x_{k+PF}
             if (xlane && k + PF < len) xr[q] = __ldg(xin + (k + PF) * W + lane);
-            letter_step<W, D>(S, xcb + (k & 1) * Lay::xcs, top, sd, c, lane);
+            letter_step<W, D>(S, xcb + (k & 1) * Lay::xcs, top, sd, c, lane, with_top);
             if (xlane && k + 1 < len) xcb[((k + 1) & 1) * Lay::xcs + lane] = xr[(q + 1) % PF];
             __syncwarp();
         }
     }
-    // the signature row: S_0 (warp 0), the slices of levels 1..D-1 and the
-    // top rows
-    float* dst = sig + b * sig_stride;
+}
+
+// Warp c's part of the signature row dst: S_0 (warp 0), the slices of levels
+// 1..D-1 and the top rows.
+template <int W, int D>
+__device__ __forceinline__ void letter_store(float* dst, const float* S,
+                                             const float (&top)[LetterLayout<W, D>::rows_per_lane][W],
+                                             const float (&sd)[LetterLayout<W, D>::rows_per_lane], uint32_t c,
+                                             uint32_t lane) {
+    using Lay = LetterLayout<W, D>;
+    constexpr int R = Lay::rows_per_lane;
     if (c == 0 && lane == 0) dst[0] = 1.0f;
 #pragma unroll
     for (int j = 1; j <= Lay::smem_levels; ++j) {
@@ -261,7 +270,313 @@ __device__ __forceinline__ void letter_path(const float* __restrict__ incr, int6
             for (int a = 0; a < W; ++a) dtop[row * W + a] = top[r][a];
         }
     }
+}
+
+// One path b with increments [off, off + len) by warp c of the path's W
+// warps, into the signature row sig + b*sig_stride.  `region` is the warp's
+// shared memory (LetterLayout::warp_floats floats: two increment buffers,
+// then the levels kept in shared memory).  Ends with __syncwarp.
+template <int W, int D>
+__device__ __forceinline__ void letter_path(const float* __restrict__ incr, int64_t b, int64_t off, int64_t len,
+                                            float* sig, int64_t sig_stride, float* region, uint32_t c,
+                                            uint32_t lane) {
+    using Lay = LetterLayout<W, D>;
+    constexpr int R = Lay::rows_per_lane;
+    float top[R][W];
+    float sd[R];
+    float* S = region + 2 * Lay::xcs;
+    letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, true);
+    letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
     __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Reverse mode with one warp per first letter (k_signature_letters_rev).
+//
+// The reverse step of signature_body.cuh restated on first-letter slices.
+// For increment x = x_k, S = S_k and the cotangent G' = G_k of S_k:
+//  * Recovery: S_{k-1} follows from S_k level by level, bottom-up, by undoing
+//    the forward Horner chains: S^-_j[u] = S_j[u] - T^j_{j-1}[p] x_a for
+//    u = (p, a), and the chains of the recovered state,
+//    T^n_j[u] = S^-_j[u] + T^n_{j-1}[p] x_a / (n-j+1) (T^n_0 = 1).
+//  * Cotangent chains, top-down: A^n_n = G'_n and
+//    A^n_{j-1}[p] = sum_a A^n_j[p a] x_a / (n-j+1); G_{k-1,j} = sum_{n>=j} A^n_j
+//    (the top level of G never changes).
+//  * Letter gradient: xbar_a = sum_{n, j, p} A^n_j[p a] T^n_{j-1}[p] / (n-j+1).
+// Every term of a word's chains involves only its prefixes, which share its
+// first letter, so warp c runs the step on its slice alone; only the letter
+// gradient sums over all slices (a butterfly in the warp, then W warps'
+// partials added in warp order once per 8 steps, after one CTA barrier).
+// Layout per warp: the seed's top rows (constant through the pass) and level
+// D-1 of S and G in registers (lane l: rows l, l + 32, ...); levels 1..D-2 of
+// S and G, the chains of levels 1..D-2 (T^n_j and T^n_j / (n-j)) and the
+// cotangent chains A^n_j of levels 1..D-1 in shared memory.  A step has 3D-4
+// warp barriers and no CTA barrier: recovery passes for levels 1..D-2; the
+// top rows (the recovery of level D-1, A^D_{D-1} and the top level's letter
+// terms, all from registers); then per level j = D-2..1 a pass over the
+// (chain n, row p) pairs (A^n_j[p] and the letter terms of p's children) and
+// one that updates G_j.
+template <int W, int D>
+struct LetterRevLayout {
+    using F = LetterLayout<W, D>;
+    static_assert(D >= 3, "level D-1 in registers");
+    static constexpr uint32_t sl(int j) { return F::slice(j); }
+    // the increment table x_a / m (m = 1..D), two of them by step parity
+    static constexpr uint32_t xs_size = (D * W + 3) / 4 * 4;
+    static constexpr uint32_t xs_off = F::warp_floats;
+    static constexpr uint32_t g_off = xs_off + 2 * xs_size;  // G levels 1..D-2 (layout of S)
+    static constexpr uint32_t tf_off = g_off + F::s_size;
+    // level j (1..D-2): T^n_j for n = j+1..D, then T^n_j / (n-j) for the same n
+    static constexpr uint32_t tf_rel(int j) {
+        uint32_t o = 0;
+        for (int i = 1; i < j; ++i) o += 2 * (D - i) * sl(i);
+        return o;
+    }
+    static constexpr uint32_t tf(int j, int n) { return tf_off + tf_rel(j) + (n - j - 1) * sl(j); }
+    static constexpr uint32_t tx(int j, int n) { return tf_off + tf_rel(j) + (D - j + n - j - 1) * sl(j); }
+    // level j (1..D-1): A^n_j for n = j..D (A^j_j: the old G_j)
+    static constexpr uint32_t ab_off = tf_off + tf_rel(D - 1);
+    static constexpr uint32_t ab_rel(int j) {
+        uint32_t o = 0;
+        for (int i = 1; i < j; ++i) o += (D - i + 1) * sl(i);
+        return o;
+    }
+    static constexpr uint32_t ab(int j, int n) { return ab_off + ab_rel(j) + (n - j) * sl(j); }
+    static constexpr uint32_t warp_floats = (ab_off + ab_rel(D) + 3) / 4 * 4;
+    static constexpr int steps_per_block = 8;  // letter partials reduced across warps once per block
+    // per CTA after the W warp regions: [2][steps_per_block][W warps][W letters]
+    static constexpr uint32_t pbuf_floats = 2u * steps_per_block * W * W;
+};
+
+// One reverse step of warp c.  `region` is the warp's shared memory, `xs` the
+// step's increment table (x_a / m at (m-1) W + a).  Adds this warp's letter
+// terms to xa.  Ends with __syncwarp.
+template <int W, int D>
+__device__ __forceinline__ void letter_reverse_step(float* region, const float* xs,
+                                                    const float (&gtop)[LetterLayout<W, D>::rows_per_lane][W],
+                                                    float (&sd)[LetterLayout<W, D>::rows_per_lane],
+                                                    float (&gd)[LetterLayout<W, D>::rows_per_lane], float (&xa)[W],
+                                                    uint32_t c, uint32_t lane) {
+    using F = LetterLayout<W, D>;
+    using Rev = LetterRevLayout<W, D>;
+    constexpr int R = F::rows_per_lane;
+    float* S = region + 2 * F::xcs;
+    float* G = region + Rev::g_off;
+    // recovery of levels 1..D-2, bottom-up, and their chains
+#pragma unroll
+    for (int j = 1; j <= D - 2; ++j) {
+        const uint32_t sl = F::slice(j);
+#pragma unroll
+        for (uint32_t q = 0; q < (sl + 31) / 32; ++q) {
+            const uint32_t u = lane + 32u * q;
+            if (u < sl) {
+                const uint32_t a = j == 1 ? c : u % W;
+                const uint32_t p = u / W;  // the prefix, in level j-1's slice (j >= 2)
+                const float s = fmaf(j == 1 ? -1.0f : -region[Rev::tf(j - 1, j) + p], xs[a], S[F::s_off(j) + u]);
+                S[F::s_off(j) + u] = s;
+#pragma unroll
+                for (int n = j + 1; n <= D; ++n) {
+                    const float par = j == 1 ? 1.0f : region[Rev::tf(j - 1, n) + p];
+                    const float t = fmaf(par, xs[(n - j) * W + a], s);
+                    region[Rev::tf(j, n) + u] = t;
+                    region[Rev::tx(j, n) + u] = __fmul_rn(t, 1.0f / static_cast<float>(n - j));
+                }
+            }
+        }
+        __syncwarp();
+    }
+    // the top rows: recovery of level D-1 (registers), T^D_{D-1}, A^D_{D-1}
+    // and the top level's letter terms
+    float x1[W];
+    if constexpr (W % 4 == 0) {
+#pragma unroll
+        for (int a = 0; a < W; a += 4) {
+            const float4 x4 = *reinterpret_cast<const float4*>(xs + a);
+            x1[a] = x4.x;
+            x1[a + 1] = x4.y;
+            x1[a + 2] = x4.z;
+            x1[a + 3] = x4.w;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < W; ++a) x1[a] = xs[a];
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        const uint32_t p = lane + 32u * q;
+        if (p < F::top_rows) {
+            const uint32_t pu = p / W, a = p % W;
+            const float s = fmaf(-region[Rev::tf(D - 2, D - 1) + pu], xs[a], sd[q]);
+            sd[q] = s;
+            const float td = fmaf(region[Rev::tf(D - 2, D) + pu], xs[W + a], s);
+            float acc = 0.0f;
+#pragma unroll
+            for (int e = 0; e < W; ++e) {
+                acc = fmaf(gtop[q][e], x1[e], acc);
+                xa[e] = fmaf(gtop[q][e], td, xa[e]);
+            }
+            region[Rev::ab(D - 1, D - 1) + p] = gd[q];
+            region[Rev::ab(D - 1, D) + p] = acc;
+            gd[q] += acc;
+        }
+    }
+    __syncwarp();
+    // levels D-2..1: the cotangent chains of each (chain n, row p) pair from
+    // p's children, with the children's letter terms; then G_j
+#pragma unroll
+    for (int j = D - 2; j >= 1; --j) {
+        const uint32_t sl = F::slice(j);
+        const uint32_t pairs = static_cast<uint32_t>(D - j) * sl;
+#pragma unroll
+        for (uint32_t q = 0; q < (pairs + 31) / 32; ++q) {
+            const uint32_t e = lane + 32u * q;  // (n - j - 1) sl + p
+            if (e < pairs) {
+                const float* ch = region + Rev::ab(j + 1, j + 1) + W * e;  // A^n_{j+1}[p a], a = 0..W-1
+                const float* xm = xs + (e / sl) * W;                        // x_a / (n - j)
+                const float tx = region[Rev::tx(j, j + 1) + e];             // T^n_j[p] / (n - j)
+                float acc = 0.0f;
+#pragma unroll
+                for (int a = 0; a < W; ++a) {
+                    const float g = ch[a];
+                    acc = fmaf(g, xm[a], acc);
+                    xa[a] = fmaf(g, tx, xa[a]);
+                }
+                region[Rev::ab(j, j) + sl + e] = acc;  // A^n_j[p]
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (uint32_t q = 0; q < (sl + 31) / 32; ++q) {
+            const uint32_t u = lane + 32u * q;
+            if (u < sl) {
+                float g = G[F::s_off(j) + u];
+                region[Rev::ab(j, j) + u] = g;  // chain n = j of level j, for level j-1
+                float term = g;                 // (j = 1) the letter term of the word c: sum_n A^n_1 / n
+#pragma unroll
+                for (int n = j + 1; n <= D; ++n) {
+                    const float an = region[Rev::ab(j, n) + u];
+                    g += an;
+                    if (j == 1) term = fmaf(an, 1.0f / static_cast<float>(n), term);
+                }
+                G[F::s_off(j) + u] = g;
+                if (j == 1) {
+#pragma unroll
+                    for (int a = 0; a < W; ++a)
+                        if (static_cast<uint32_t>(a) == c) xa[a] += term;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Forward and reverse pass of one path by warp c (k_signature_letters_rev).
+// Modes: kForward | kBackward [| kTopLevel] (the forward pass first, writing
+// the signature row with kTopLevel) and kBackward | kLoadFinal (the final
+// signature read from sig).  `pbuf` is the CTA's partials buffer
+// (LetterRevLayout::pbuf_floats), `region` the warp's shared memory
+// (LetterRevLayout::warp_floats).  Contains CTA barriers: every warp of the
+// CTA runs the same path.
+template <int W, int D>
+__device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, int64_t b, int64_t off, int64_t len,
+                                               float* sig, int64_t sig_stride, const float* __restrict__ seed,
+                                               int64_t seed_stride, float* grad, int mode, float* region,
+                                               float* pbuf, uint32_t c, uint32_t lane) {
+    using F = LetterLayout<W, D>;
+    using Rev = LetterRevLayout<W, D>;
+    constexpr int R = F::rows_per_lane;
+    constexpr int PF = Rev::steps_per_block;  // increments prefetched ahead = steps per partials block
+    float* S = region + 2 * F::xcs;
+    float sd[R];
+    if (mode & kLoadFinal) {
+        const float* src = sig + b * sig_stride;
+#pragma unroll
+        for (int j = 1; j <= D - 2; ++j)
+            for (uint32_t u = lane; u < F::slice(j); u += 32)
+                S[F::s_off(j) + u] = src[level_start<W>(j) + c * F::slice(j) + u];
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const uint32_t p = lane + 32u * q;
+            sd[q] = p < F::top_rows ? src[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
+        }
+        __syncwarp();
+    } else {
+        float top[R][W];
+        const bool with_top = mode & kTopLevel;
+        letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, with_top);
+        if (with_top && sig) letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
+    }
+    // the seed: top rows and level D-1 to registers, levels 1..D-2 to G
+    const float* sdr = seed + b * seed_stride;
+    float* G = region + Rev::g_off;
+    float gtop[R][W], gd[R];
+#pragma unroll
+    for (int j = 1; j <= D - 2; ++j)
+        for (uint32_t u = lane; u < F::slice(j); u += 32)
+            G[F::s_off(j) + u] = sdr[level_start<W>(j) + c * F::slice(j) + u];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        const uint32_t p = lane + 32u * q;
+        const bool row = p < F::top_rows;
+        gd[q] = row ? sdr[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
+#pragma unroll
+        for (int a = 0; a < W; ++a) gtop[q][a] = row ? sdr[level_start<W>(D) + c * F::slice(D) + p * W + a] : 0.0f;
+    }
+    // increments from the last: lane a < W loads letter a PF steps ahead;
+    // lane l < D W writes entry l of the table, x_{l % W} / (l / W + 1)
+    const bool xlane = lane < static_cast<uint32_t>(W);
+    const bool tlane = lane < static_cast<uint32_t>(D * W);
+    const uint32_t src_lane = lane % W;
+    const float inv_m = 1.0f / static_cast<float>(lane / W + 1);
+    const float* xin = incr + off * W;
+    float* xsb = region + Rev::xs_off;
+    float* gout = grad + off * W;
+    float xr[PF];
+#pragma unroll
+    for (int q = 0; q < PF; ++q) xr[q] = (xlane && q < len) ? __ldg(xin + (len - 1 - q) * W + lane) : 0.0f;
+    {
+        const float v = __shfl_sync(0xffffffffu, xr[0], src_lane);
+        if (tlane && len > 0) xsb[lane] = __fmul_rn(v, inv_m);
+    }
+    __syncwarp();
+    float xa[W];
+#pragma unroll
+    for (int a = 0; a < W; ++a) xa[a] = 0.0f;
+    constexpr uint32_t halvings = W <= 1 ? 0u : W <= 2 ? 1u : W <= 4 ? 2u : W <= 8 ? 3u : 4u;
+    for (int64_t i0 = 0; i0 < len; i0 += PF) {
+        float* pb = pbuf + ((i0 / PF) & 1) * (PF * W * W);
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            const int64_t i = i0 + q;  // reverse step i: increment len - 1 - i
+            if (i >= len) break;
+            if (xlane && i + PF < len) xr[q] = __ldg(xin + (len - 1 - i - PF) * W + lane);
+            letter_reverse_step<W, D>(region, xsb + (i & 1) * Rev::xs_size, gtop, sd, gd, xa, c, lane);
+            {  // the next step's table (the other buffer)
+                const float v = __shfl_sync(0xffffffffu, xr[(q + 1) % PF], src_lane);
+                if (tlane && i + 1 < len) xsb[((i + 1) & 1) * Rev::xs_size + lane] = __fmul_rn(v, inv_m);
+            }
+            // this warp's letter partials: pb[q][c][a]
+            uint32_t base = 0, cnt = W;
+            letter_butterfly<float, W>(xa, lane, 16u, base, cnt);
+            if (cnt > 0u && (lane & ((32u >> halvings) - 1u)) == 0u) pb[(q * W + c) * W + base] = xa[0];
+#pragma unroll
+            for (int a = 0; a < W; ++a) xa[a] = 0.0f;
+            __syncwarp();
+            if (q == PF - 1 || i == len - 1) {
+                // the block's gradient rows: the W warps' partials added in
+                // warp order (the other half of pbuf takes the next block)
+                __syncthreads();
+                const uint32_t t = threadIdx.x;
+                if (t < static_cast<uint32_t>(q + 1) * W) {
+                    const uint32_t st = t / W, a = t % W;
+                    float v = 0.0f;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) v += pb[(st * W + w) * W + a];
+                    gout[(len - 1 - (i0 + st)) * W + a] = v;
+                }
+            }
+        }
+    }
 }
 
 // The instantiated (width, depth) shapes, as X(width, depth) entries: at most

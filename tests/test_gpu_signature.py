@@ -504,3 +504,89 @@ def test_fp32_one_warp_per_letter_equals_shared_memory_kernel(W, D):
     for k in (1, 2):
         diff = float(torch.max(torch.abs(out[0] - out[k])).item())
         assert torch.equal(out[0], out[k]), f"W{W} D{D}: schedule {k} differs by up to {diff:.3e}"
+
+
+LETTER_REV_SHAPES = [(8, 4), (5, 5), (5, 3), (4, 5), (6, 4), (3, 6), (8, 3), (4, 4), (3, 5), (5, 4)]
+
+
+def letter_rev_case(W, D, ragged, seed):
+    rng = np.random.default_rng(seed)
+    B, L = 13, 9
+    if ragged:
+        lengths = np.array([0, 1, 2, 17, 5, 0, 9, 31, 1, 4, 12, 3, 8])
+        offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    else:
+        offsets = np.arange(B + 1, dtype=np.int64) * L
+    incr = rng.normal(0, 1 / np.sqrt(L), (int(offsets[-1]), W))
+    ell = rng.uniform(-1, 1, (B, O.tensor_dim(W, D)))
+    return B, offsets, incr, ell
+
+
+@pytest.mark.parametrize("W,D", LETTER_REV_SHAPES)
+@pytest.mark.parametrize("ragged", [False, True])
+def test_fp32_reverse_one_warp_per_letter(orc, W, D, ragged):
+    """FP32 forward + reverse with one warp per first letter (schedule bit 16 on
+    a call with a reverse pass): signatures and increment gradients against the
+    FP64 oracle at 1e-5; ragged batches with empty and unit paths, and lengths
+    on both sides of the 8-step blocks in which the letter gradients are added
+    across warps."""
+    B, offsets, incr, ell = letter_rev_case(W, D, ragged, W * 53 + D)
+    basis = pkg.TensorBasis(W, D)
+    st = pkg.GB300Strategy(torch.float32)
+    sig = torch.full((B, basis.size()), float("nan"), dtype=torch.float32, device="cuda")
+    grad = torch.full(incr.shape, float("nan"), dtype=torch.float32, device="cuda")
+    kw = dict(offsets=dev(offsets, torch.int64)) if ragged else dict(length=int(offsets[1]))
+    err = pkg.signature(st, None, dev(incr, torch.float32), basis, B, out=sig, seed=dev(ell, torch.float32),
+                        grad=grad, schedule=32 | (1 << 16), **kw)
+    assert err, err.message
+    esig, egrad = orc.signature(W, D, incr, offsets, ell=ell)
+    assert_close(host(sig), esig, TOL_F32, f"FP32 letter warps W{W} D{D} signature")
+    e = scaled_err(host(grad), egrad)
+    assert e <= TOL_F32, f"FP32 letter warps W{W} D{D} gradient: scaled error {e:.3e}"
+
+
+@pytest.mark.parametrize("W,D", [(5, 5), (8, 4), (3, 6)])
+def test_fp32_reverse_one_warp_per_letter_gradient_only_and_backward_entry(orc, W, D):
+    """The same kernel without signature output (its forward pass skips the top
+    level) and from given final signatures (rpp_gb_signature_backward, whose
+    FP32 calls of these shapes take it without a recorded schedule)."""
+    B, offsets, incr, ell = letter_rev_case(W, D, True, W * 59 + D)
+    basis = pkg.TensorBasis(W, D)
+    st = pkg.GB300Strategy(torch.float32)
+    offs = dev(offsets, torch.int64)
+    esig, egrad = orc.signature(W, D, incr, offsets, ell=ell)
+    grad = torch.full(incr.shape, float("nan"), dtype=torch.float32, device="cuda")
+    err = pkg.signature(st, None, dev(incr, torch.float32), basis, B, offsets=offs, seed=dev(ell, torch.float32),
+                        grad=grad, schedule=32 | (1 << 16))
+    assert err, err.message
+    e = scaled_err(host(grad), egrad)
+    assert e <= TOL_F32, f"gradient-only W{W} D{D}: scaled error {e:.3e}"
+    g2 = torch.full(incr.shape, float("nan"), dtype=torch.float32, device="cuda")
+    err = pkg.signature_backward(st, None, dev(incr, torch.float32), basis, B, dev(esig, torch.float32),
+                                 dev(ell, torch.float32), g2, offsets=offs)
+    assert err, err.message
+    e = scaled_err(host(g2), egrad)
+    assert e <= TOL_F32, f"backward entry W{W} D{D}: scaled error {e:.3e}"
+
+
+@pytest.mark.parametrize("W,D", [(5, 5), (8, 4), (4, 5)])
+def test_fp32_reverse_one_warp_per_letter_agrees_with_shared_memory_kernel(W, D):
+    """The warp-per-letter reverse pass sums the same terms as the shared-memory
+    kernel in another order (the letter gradients per slice, then across
+    slices): the two agree to a few FP32 roundings, at the headline length."""
+    rng = np.random.default_rng(W * 61 + D)
+    B, L = 24, 256
+    incr = dev(rng.normal(0, 1 / np.sqrt(L), (B * L, W)), torch.float32)
+    basis = pkg.TensorBasis(W, D)
+    ell = dev(rng.uniform(-1, 1, (B, basis.size())), torch.float32)
+    st = pkg.GB300Strategy(torch.float32)
+    out = []
+    for schedule in (32 | (1 << 16), 256):
+        sig = torch.full((B, basis.size()), float("nan"), dtype=torch.float32, device="cuda")
+        grad = torch.full((B * L, W), float("nan"), dtype=torch.float32, device="cuda")
+        err = pkg.signature(st, None, incr, basis, B, length=L, out=sig, seed=ell, grad=grad, schedule=schedule)
+        assert err, err.message
+        out.append((host(sig), host(grad)))
+    assert np.array_equal(out[0][0], out[1][0]), "signatures differ"
+    e = scaled_err(out[0][1], out[1][1])
+    assert e <= 2e-6, f"W{W} D{D}: gradients differ by {e:.3e} (scaled)"
