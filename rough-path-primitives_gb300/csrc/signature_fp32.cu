@@ -45,10 +45,11 @@ __global__ void __launch_bounds__(W * 32, letter_min_blocks(W, D)) k_signature_l
     }
 }
 
-// Registers for the reverse kernel: 24 warps per SM (about 85 registers a
-// thread: the seed's top rows, levels D-1 of S and G, the letter sums and the
-// increment ring).
-constexpr int letter_rev_min_blocks(int W) { return 768 / (W * 32) > 0 ? 768 / (W * 32) : 1; }
+// Registers for the reverse kernel: 20 warps per SM, about 100 registers a
+// thread (the seed's top rows, level D-1 and the lane's lower coefficients of
+// S and G, the letter sums and the increment ring; at 24 warps per SM, W8 D4
+// and W3 D6 spilled).
+constexpr int letter_rev_min_blocks(int W) { return 640 / (W * 32) > 0 ? 640 / (W * 32) : 1; }
 
 // Forward + reverse (or reverse from the final signature) with one warp per
 // first letter: a CTA of W warps runs one path at a time.

@@ -307,13 +307,16 @@ __device__ __forceinline__ void letter_path(const float* __restrict__ incr, int6
 // first letter, so warp c runs the step on its slice alone; only the letter
 // gradient sums over all slices (a butterfly in the warp, then W warps'
 // partials added in warp order once per 8 steps, after one CTA barrier).
-// Layout per warp: the seed's top rows (constant through the pass) and level
-// D-1 of S and G in registers (lane l: rows l, l + 32, ...); levels 1..D-2 of
-// S and G, the chains of levels 1..D-2 (T^n_j and T^n_j / (n-j)) and the
-// cotangent chains A^n_j of levels 1..D-1 in shared memory.  A step has 3D-4
-// warp barriers and no CTA barrier: recovery passes for levels 1..D-2; the
-// top rows (the recovery of level D-1, A^D_{D-1} and the top level's letter
-// terms, all from registers); then per level j = D-2..1 a pass over the
+// The kernel is bound by shared-memory instructions, so everything a lane
+// alone reads lives in its registers: the seed's top rows (constant through
+// the pass), and of S and G level D-1 (lane l: rows l, l + 32, ...) and the
+// lane's own coefficients of levels 1..D-2 (l, l + 32, ... of each level).
+// Scaled increments x_a / m are formed in registers (x_a * (1/m), rounded
+// once).  Shared memory holds only what other lanes read: the increment, the
+// chains T^n_j of levels 1..D-2 and the cotangent chains A^n_j of levels
+// 1..D-1.  A step has 3D-4 warp barriers and no CTA barrier: recovery passes
+// for levels 1..D-2; the top rows (the recovery of level D-1, A^D_{D-1} and
+// the top level's letter terms); then per level j = D-2..1 a pass over the
 // (chain n, row p) pairs (A^n_j[p] and the letter terms of p's children) and
 // one that updates G_j.
 template <int W, int D>
@@ -321,19 +324,15 @@ struct LetterRevLayout {
     using F = LetterLayout<W, D>;
     static_assert(D >= 3, "level D-1 in registers");
     static constexpr uint32_t sl(int j) { return F::slice(j); }
-    // the increment table x_a / m (m = 1..D), two of them by step parity
-    static constexpr uint32_t xs_size = (D * W + 3) / 4 * 4;
-    static constexpr uint32_t xs_off = F::warp_floats;
-    static constexpr uint32_t g_off = xs_off + 2 * xs_size;  // G levels 1..D-2 (layout of S)
-    static constexpr uint32_t tf_off = g_off + F::s_size;
-    // level j (1..D-2): T^n_j for n = j+1..D, then T^n_j / (n-j) for the same n
+    static constexpr uint32_t xb_off = F::warp_floats;  // two increment buffers, by step parity
+    static constexpr uint32_t tf_off = xb_off + 2 * F::xcs;
+    // level j (1..D-2): T^n_j for n = j+1..D
     static constexpr uint32_t tf_rel(int j) {
         uint32_t o = 0;
-        for (int i = 1; i < j; ++i) o += 2 * (D - i) * sl(i);
+        for (int i = 1; i < j; ++i) o += (D - i) * sl(i);
         return o;
     }
     static constexpr uint32_t tf(int j, int n) { return tf_off + tf_rel(j) + (n - j - 1) * sl(j); }
-    static constexpr uint32_t tx(int j, int n) { return tf_off + tf_rel(j) + (D - j + n - j - 1) * sl(j); }
     // level j (1..D-1): A^n_j for n = j..D (A^j_j: the old G_j)
     static constexpr uint32_t ab_off = tf_off + tf_rel(D - 1);
     static constexpr uint32_t ab_rel(int j) {
@@ -343,25 +342,41 @@ struct LetterRevLayout {
     }
     static constexpr uint32_t ab(int j, int n) { return ab_off + ab_rel(j) + (n - j) * sl(j); }
     static constexpr uint32_t warp_floats = (ab_off + ab_rel(D) + 3) / 4 * 4;
+    // registers: the lane's coefficients of levels 1..D-2 (lo), and the
+    // scale 1 / (n - j) of each (chain n, row) pair the lane takes (pr)
+    static constexpr int lo(int j) {
+        int o = 0;
+        for (int i = 1; i < j; ++i) o += static_cast<int>((sl(i) + 31) / 32);
+        return o;
+    }
+    static constexpr int pr(int j) {
+        int o = 0;
+        for (int i = 1; i < j; ++i) o += static_cast<int>(((D - i) * sl(i) + 31) / 32);
+        return o;
+    }
+    static constexpr int lo_total = lo(D - 1) > 0 ? lo(D - 1) : 1;
+    static constexpr int pr_total = pr(D - 1) > 0 ? pr(D - 1) : 1;
     static constexpr int steps_per_block = 8;  // letter partials reduced across warps once per block
     // per CTA after the W warp regions: [2][steps_per_block][W warps][W letters]
     static constexpr uint32_t pbuf_floats = 2u * steps_per_block * W * W;
 };
 
-// One reverse step of warp c.  `region` is the warp's shared memory, `xs` the
-// step's increment table (x_a / m at (m-1) W + a).  Adds this warp's letter
-// terms to xa.  Ends with __syncwarp.
+// One reverse step of warp c.  `region` is the warp's shared memory, `xb` the
+// step's increment (x_a at a).  slo / glo: the lane's coefficients of S and G
+// on levels 1..D-2; pinv: its pair scales.  Adds this warp's letter terms to
+// xa.  Ends with __syncwarp.
 template <int W, int D>
-__device__ __forceinline__ void letter_reverse_step(float* region, const float* xs,
+__device__ __forceinline__ void letter_reverse_step(float* region, const float* xb,
                                                     const float (&gtop)[LetterLayout<W, D>::rows_per_lane][W],
                                                     float (&sd)[LetterLayout<W, D>::rows_per_lane],
-                                                    float (&gd)[LetterLayout<W, D>::rows_per_lane], float (&xa)[W],
-                                                    uint32_t c, uint32_t lane) {
+                                                    float (&gd)[LetterLayout<W, D>::rows_per_lane],
+                                                    float (&slo)[LetterRevLayout<W, D>::lo_total],
+                                                    float (&glo)[LetterRevLayout<W, D>::lo_total],
+                                                    const float (&pinv)[LetterRevLayout<W, D>::pr_total],
+                                                    float (&xa)[W], uint32_t c, uint32_t lane) {
     using F = LetterLayout<W, D>;
     using Rev = LetterRevLayout<W, D>;
     constexpr int R = F::rows_per_lane;
-    float* S = region + 2 * F::xcs;
-    float* G = region + Rev::g_off;
     // recovery of levels 1..D-2, bottom-up, and their chains
 #pragma unroll
     for (int j = 1; j <= D - 2; ++j) {
@@ -372,14 +387,13 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
             if (u < sl) {
                 const uint32_t a = j == 1 ? c : u % W;
                 const uint32_t p = u / W;  // the prefix, in level j-1's slice (j >= 2)
-                const float s = fmaf(j == 1 ? -1.0f : -region[Rev::tf(j - 1, j) + p], xs[a], S[F::s_off(j) + u]);
-                S[F::s_off(j) + u] = s;
+                const float xv = xb[a];
+                const float s = fmaf(j == 1 ? -1.0f : -region[Rev::tf(j - 1, j) + p], xv, slo[Rev::lo(j) + q]);
+                slo[Rev::lo(j) + q] = s;
 #pragma unroll
                 for (int n = j + 1; n <= D; ++n) {
                     const float par = j == 1 ? 1.0f : region[Rev::tf(j - 1, n) + p];
-                    const float t = fmaf(par, xs[(n - j) * W + a], s);
-                    region[Rev::tf(j, n) + u] = t;
-                    region[Rev::tx(j, n) + u] = __fmul_rn(t, 1.0f / static_cast<float>(n - j));
+                    region[Rev::tf(j, n) + u] = fmaf(par, __fmul_rn(xv, 1.0f / static_cast<float>(n - j + 1)), s);
                 }
             }
         }
@@ -391,7 +405,7 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
     if constexpr (W % 4 == 0) {
 #pragma unroll
         for (int a = 0; a < W; a += 4) {
-            const float4 x4 = *reinterpret_cast<const float4*>(xs + a);
+            const float4 x4 = *reinterpret_cast<const float4*>(xb + a);
             x1[a] = x4.x;
             x1[a + 1] = x4.y;
             x1[a + 2] = x4.z;
@@ -399,16 +413,17 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
         }
     } else {
 #pragma unroll
-        for (int a = 0; a < W; ++a) x1[a] = xs[a];
+        for (int a = 0; a < W; ++a) x1[a] = xb[a];
     }
 #pragma unroll
     for (int q = 0; q < R; ++q) {
         const uint32_t p = lane + 32u * q;
         if (p < F::top_rows) {
             const uint32_t pu = p / W, a = p % W;
-            const float s = fmaf(-region[Rev::tf(D - 2, D - 1) + pu], xs[a], sd[q]);
+            const float xl = xb[a];
+            const float s = fmaf(-region[Rev::tf(D - 2, D - 1) + pu], xl, sd[q]);
             sd[q] = s;
-            const float td = fmaf(region[Rev::tf(D - 2, D) + pu], xs[W + a], s);
+            const float td = fmaf(region[Rev::tf(D - 2, D) + pu], __fmul_rn(xl, 0.5f), s);
             float acc = 0.0f;
 #pragma unroll
             for (int e = 0; e < W; ++e) {
@@ -431,14 +446,14 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
         for (uint32_t q = 0; q < (pairs + 31) / 32; ++q) {
             const uint32_t e = lane + 32u * q;  // (n - j - 1) sl + p
             if (e < pairs) {
+                const float inv = pinv[Rev::pr(j) + q];                     // 1 / (n - j)
                 const float* ch = region + Rev::ab(j + 1, j + 1) + W * e;  // A^n_{j+1}[p a], a = 0..W-1
-                const float* xm = xs + (e / sl) * W;                        // x_a / (n - j)
-                const float tx = region[Rev::tx(j, j + 1) + e];             // T^n_j[p] / (n - j)
+                const float tx = __fmul_rn(region[Rev::tf(j, j + 1) + e], inv);  // T^n_j[p] / (n - j)
                 float acc = 0.0f;
 #pragma unroll
                 for (int a = 0; a < W; ++a) {
                     const float g = ch[a];
-                    acc = fmaf(g, xm[a], acc);
+                    acc = fmaf(g, __fmul_rn(x1[a], inv), acc);
                     xa[a] = fmaf(g, tx, xa[a]);
                 }
                 region[Rev::ab(j, j) + sl + e] = acc;  // A^n_j[p]
@@ -449,7 +464,7 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
         for (uint32_t q = 0; q < (sl + 31) / 32; ++q) {
             const uint32_t u = lane + 32u * q;
             if (u < sl) {
-                float g = G[F::s_off(j) + u];
+                float g = glo[Rev::lo(j) + q];
                 region[Rev::ab(j, j) + u] = g;  // chain n = j of level j, for level j-1
                 float term = g;                 // (j = 1) the letter term of the word c: sum_n A^n_1 / n
 #pragma unroll
@@ -458,7 +473,7 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
                     g += an;
                     if (j == 1) term = fmaf(an, 1.0f / static_cast<float>(n), term);
                 }
-                G[F::s_off(j) + u] = g;
+                glo[Rev::lo(j) + q] = g;
                 if (j == 1) {
 #pragma unroll
                     for (int a = 0; a < W; ++a)
@@ -485,35 +500,48 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
     using F = LetterLayout<W, D>;
     using Rev = LetterRevLayout<W, D>;
     constexpr int R = F::rows_per_lane;
-    constexpr int PF = Rev::steps_per_block;  // increments prefetched ahead = steps per partials block
+    constexpr int NB = Rev::steps_per_block;  // steps per partials block
+    constexpr int PF = 4;                     // increments prefetched ahead (NB a multiple)
     float* S = region + 2 * F::xcs;
     float sd[R];
+    float slo[Rev::lo_total], glo[Rev::lo_total];
     if (mode & kLoadFinal) {
         const float* src = sig + b * sig_stride;
 #pragma unroll
         for (int j = 1; j <= D - 2; ++j)
-            for (uint32_t u = lane; u < F::slice(j); u += 32)
-                S[F::s_off(j) + u] = src[level_start<W>(j) + c * F::slice(j) + u];
+#pragma unroll
+            for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
+                const uint32_t u = lane + 32u * q;
+                slo[Rev::lo(j) + q] = u < F::slice(j) ? src[level_start<W>(j) + c * F::slice(j) + u] : 0.0f;
+            }
 #pragma unroll
         for (int q = 0; q < R; ++q) {
             const uint32_t p = lane + 32u * q;
             sd[q] = p < F::top_rows ? src[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
         }
-        __syncwarp();
     } else {
         float top[R][W];
         const bool with_top = mode & kTopLevel;
         letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, with_top);
         if (with_top && sig) letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
+#pragma unroll
+        for (int j = 1; j <= D - 2; ++j)
+#pragma unroll
+            for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
+                const uint32_t u = lane + 32u * q;
+                slo[Rev::lo(j) + q] = u < F::slice(j) ? S[F::s_off(j) + u] : 0.0f;
+            }
     }
-    // the seed: top rows and level D-1 to registers, levels 1..D-2 to G
+    // the seed: top rows, level D-1 and the lane's lower coefficients
     const float* sdr = seed + b * seed_stride;
-    float* G = region + Rev::g_off;
     float gtop[R][W], gd[R];
 #pragma unroll
     for (int j = 1; j <= D - 2; ++j)
-        for (uint32_t u = lane; u < F::slice(j); u += 32)
-            G[F::s_off(j) + u] = sdr[level_start<W>(j) + c * F::slice(j) + u];
+#pragma unroll
+        for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
+            const uint32_t u = lane + 32u * q;
+            glo[Rev::lo(j) + q] = u < F::slice(j) ? sdr[level_start<W>(j) + c * F::slice(j) + u] : 0.0f;
+        }
 #pragma unroll
     for (int q = 0; q < R; ++q) {
         const uint32_t p = lane + 32u * q;
@@ -522,39 +550,39 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
 #pragma unroll
         for (int a = 0; a < W; ++a) gtop[q][a] = row ? sdr[level_start<W>(D) + c * F::slice(D) + p * W + a] : 0.0f;
     }
-    // increments from the last: lane a < W loads letter a PF steps ahead;
-    // lane l < D W writes entry l of the table, x_{l % W} / (l / W + 1)
+    // the scale 1 / (n - j) of each (chain n, row) pair of level j this lane
+    // takes: pair e = lane + 32 q, n - j = e / W^{j-1} + 1
+    float pinv[Rev::pr_total];
+#pragma unroll
+    for (int j = 1; j <= D - 2; ++j)
+#pragma unroll
+        for (uint32_t q = 0; q < ((D - j) * F::slice(j) + 31) / 32; ++q)
+            pinv[Rev::pr(j) + q] = 1.0f / static_cast<float>((lane + 32u * q) / F::slice(j) + 1);
+    // increments from the last: lane a < W loads letter a PF steps ahead
     const bool xlane = lane < static_cast<uint32_t>(W);
-    const bool tlane = lane < static_cast<uint32_t>(D * W);
-    const uint32_t src_lane = lane % W;
-    const float inv_m = 1.0f / static_cast<float>(lane / W + 1);
     const float* xin = incr + off * W;
-    float* xsb = region + Rev::xs_off;
+    float* xbuf = region + Rev::xb_off;
     float* gout = grad + off * W;
     float xr[PF];
 #pragma unroll
     for (int q = 0; q < PF; ++q) xr[q] = (xlane && q < len) ? __ldg(xin + (len - 1 - q) * W + lane) : 0.0f;
-    {
-        const float v = __shfl_sync(0xffffffffu, xr[0], src_lane);
-        if (tlane && len > 0) xsb[lane] = __fmul_rn(v, inv_m);
-    }
+    if (xlane && len > 0) xbuf[lane] = xr[0];
     __syncwarp();
     float xa[W];
 #pragma unroll
     for (int a = 0; a < W; ++a) xa[a] = 0.0f;
     constexpr uint32_t halvings = W <= 1 ? 0u : W <= 2 ? 1u : W <= 4 ? 2u : W <= 8 ? 3u : 4u;
-    for (int64_t i0 = 0; i0 < len; i0 += PF) {
-        float* pb = pbuf + ((i0 / PF) & 1) * (PF * W * W);
+    for (int64_t i0 = 0; i0 < len; i0 += NB) {
+        float* pb = pbuf + ((i0 / NB) & 1) * (NB * W * W);
 #pragma unroll
-        for (int q = 0; q < PF; ++q) {
+        for (int q = 0; q < NB; ++q) {
             const int64_t i = i0 + q;  // reverse step i: increment len - 1 - i
             if (i >= len) break;
-            if (xlane && i + PF < len) xr[q] = __ldg(xin + (len - 1 - i - PF) * W + lane);
-            letter_reverse_step<W, D>(region, xsb + (i & 1) * Rev::xs_size, gtop, sd, gd, xa, c, lane);
-            {  // the next step's table (the other buffer)
-                const float v = __shfl_sync(0xffffffffu, xr[(q + 1) % PF], src_lane);
-                if (tlane && i + 1 < len) xsb[((i + 1) & 1) * Rev::xs_size + lane] = __fmul_rn(v, inv_m);
-            }
+            // ring slot q % PF held increment i (now in the buffer): refill
+            // it with increment i + PF
+            if (xlane && i + PF < len) xr[q % PF] = __ldg(xin + (len - 1 - i - PF) * W + lane);
+            letter_reverse_step<W, D>(region, xbuf + (i & 1) * F::xcs, gtop, sd, gd, slo, glo, pinv, xa, c, lane);
+            if (xlane && i + 1 < len) xbuf[((i + 1) & 1) * F::xcs + lane] = xr[(q + 1) % PF];
             // this warp's letter partials: pb[q][c][a]
             uint32_t base = 0, cnt = W;
             letter_butterfly<float, W>(xa, lane, 16u, base, cnt);
@@ -562,7 +590,7 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
 #pragma unroll
             for (int a = 0; a < W; ++a) xa[a] = 0.0f;
             __syncwarp();
-            if (q == PF - 1 || i == len - 1) {
+            if (q == NB - 1 || i == len - 1) {
                 // the block's gradient rows: the W warps' partials added in
                 // warp order (the other half of pbuf takes the next block)
                 __syncthreads();
