@@ -314,11 +314,11 @@ __device__ __forceinline__ void letter_path(const float* __restrict__ incr, int6
 // Scaled increments x_a / m are formed in registers (x_a * (1/m), rounded
 // once).  Shared memory holds only what other lanes read: the increment, the
 // chains T^n_j of levels 1..D-2 and the cotangent chains A^n_j of levels
-// 1..D-1.  A step has 3D-4 warp barriers and no CTA barrier: recovery passes
+// 1..D-1.  A step has 2D-2 warp barriers and no CTA barrier: recovery passes
 // for levels 1..D-2; the top rows (the recovery of level D-1, A^D_{D-1} and
-// the top level's letter terms); then per level j = D-2..1 a pass over the
-// (chain n, row p) pairs (A^n_j[p] and the letter terms of p's children) and
-// one that updates G_j.
+// the top level's letter terms); per level j = D-2..1 a pass over the
+// (chain n, row p) pairs (A^n_j[p] and the letter terms of p's children);
+// and one that updates G on levels 1..D-2.
 template <int W, int D>
 struct LetterRevLayout {
     using F = LetterLayout<W, D>;
@@ -437,7 +437,8 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
     }
     __syncwarp();
     // levels D-2..1: the cotangent chains of each (chain n, row p) pair from
-    // p's children, with the children's letter terms; then G_j
+    // p's children (chain n = j+1 of level j+1: G_{j+1} as of the step's
+    // start), with the children's letter terms
 #pragma unroll
     for (int j = D - 2; j >= 1; --j) {
         const uint32_t sl = F::slice(j);
@@ -460,13 +461,20 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
             }
         }
         __syncwarp();
+    }
+    // G_j += sum_{n>j} A^n_j on levels 1..D-2 (the lane's own coefficients),
+    // the new value copied to chain n = j of level j for the next step's
+    // pass over level j-1; and the letter term of the word c,
+    // sum_n A^n_1 / n with A^1_1 the old G_1
+#pragma unroll
+    for (int j = 1; j <= D - 2; ++j) {
+        const uint32_t sl = F::slice(j);
 #pragma unroll
         for (uint32_t q = 0; q < (sl + 31) / 32; ++q) {
             const uint32_t u = lane + 32u * q;
             if (u < sl) {
                 float g = glo[Rev::lo(j) + q];
-                region[Rev::ab(j, j) + u] = g;  // chain n = j of level j, for level j-1
-                float term = g;                 // (j = 1) the letter term of the word c: sum_n A^n_1 / n
+                float term = g;
 #pragma unroll
                 for (int n = j + 1; n <= D; ++n) {
                     const float an = region[Rev::ab(j, n) + u];
@@ -474,6 +482,7 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
                     if (j == 1) term = fmaf(an, 1.0f / static_cast<float>(n), term);
                 }
                 glo[Rev::lo(j) + q] = g;
+                region[Rev::ab(j, j) + u] = g;
                 if (j == 1) {
 #pragma unroll
                     for (int a = 0; a < W; ++a)
@@ -481,8 +490,8 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
                 }
             }
         }
-        __syncwarp();
     }
+    __syncwarp();
 }
 
 // Forward and reverse pass of one path by warp c (k_signature_letters_rev).
@@ -501,7 +510,7 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
     using Rev = LetterRevLayout<W, D>;
     constexpr int R = F::rows_per_lane;
     constexpr int NB = Rev::steps_per_block;  // steps per partials block
-    constexpr int PF = 4;                     // increments prefetched ahead (NB a multiple)
+    constexpr int PF = 4;                     // increments prefetched ahead = steps per loop iteration
     float* S = region + 2 * F::xcs;
     float sd[R];
     float slo[Rev::lo_total], glo[Rev::lo_total];
@@ -550,6 +559,14 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
 #pragma unroll
         for (int a = 0; a < W; ++a) gtop[q][a] = row ? sdr[level_start<W>(D) + c * F::slice(D) + p * W + a] : 0.0f;
     }
+    // chain n = j of each level j <= D-2: G_j as of the first step's start
+#pragma unroll
+    for (int j = 1; j <= D - 2; ++j)
+#pragma unroll
+        for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
+            const uint32_t u = lane + 32u * q;
+            if (u < F::slice(j)) region[Rev::ab(j, j) + u] = glo[Rev::lo(j) + q];
+        }
     // the scale 1 / (n - j) of each (chain n, row) pair of level j this lane
     // takes: pair e = lane + 32 q, n - j = e / W^{j-1} + 1
     float pinv[Rev::pr_total];
@@ -572,35 +589,36 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
 #pragma unroll
     for (int a = 0; a < W; ++a) xa[a] = 0.0f;
     constexpr uint32_t halvings = W <= 1 ? 0u : W <= 2 ? 1u : W <= 4 ? 2u : W <= 8 ? 3u : 4u;
-    for (int64_t i0 = 0; i0 < len; i0 += NB) {
-        float* pb = pbuf + ((i0 / NB) & 1) * (NB * W * W);
+    for (int64_t i0 = 0; i0 < len; i0 += PF) {
 #pragma unroll
-        for (int q = 0; q < NB; ++q) {
+        for (int q = 0; q < PF; ++q) {
             const int64_t i = i0 + q;  // reverse step i: increment len - 1 - i
             if (i >= len) break;
-            // ring slot q % PF held increment i (now in the buffer): refill
-            // it with increment i + PF
-            if (xlane && i + PF < len) xr[q % PF] = __ldg(xin + (len - 1 - i - PF) * W + lane);
+            // ring slot q held increment i (now in the buffer): refill it
+            // with increment i + PF
+            if (xlane && i + PF < len) xr[q] = __ldg(xin + (len - 1 - i - PF) * W + lane);
             letter_reverse_step<W, D>(region, xbuf + (i & 1) * F::xcs, gtop, sd, gd, slo, glo, pinv, xa, c, lane);
             if (xlane && i + 1 < len) xbuf[((i + 1) & 1) * F::xcs + lane] = xr[(q + 1) % PF];
+            const uint32_t slot = static_cast<uint32_t>(i % NB);
+            float* pb = pbuf + ((i / NB) & 1) * (NB * W * W);
             // this warp's letter partials: pb[q][c][a]
             uint32_t base = 0, cnt = W;
             letter_butterfly<float, W>(xa, lane, 16u, base, cnt);
-            if (cnt > 0u && (lane & ((32u >> halvings) - 1u)) == 0u) pb[(q * W + c) * W + base] = xa[0];
+            if (cnt > 0u && (lane & ((32u >> halvings) - 1u)) == 0u) pb[(slot * W + c) * W + base] = xa[0];
 #pragma unroll
             for (int a = 0; a < W; ++a) xa[a] = 0.0f;
             __syncwarp();
-            if (q == NB - 1 || i == len - 1) {
+            if (slot == NB - 1 || i == len - 1) {
                 // the block's gradient rows: the W warps' partials added in
                 // warp order (the other half of pbuf takes the next block)
                 __syncthreads();
                 const uint32_t t = threadIdx.x;
-                if (t < static_cast<uint32_t>(q + 1) * W) {
+                if (t < (slot + 1) * W) {
                     const uint32_t st = t / W, a = t % W;
                     float v = 0.0f;
 #pragma unroll
                     for (int w = 0; w < W; ++w) v += pb[(st * W + w) * W + a];
-                    gout[(len - 1 - (i0 + st)) * W + a] = v;
+                    gout[(len - 1 - (i - slot + st)) * W + a] = v;
                 }
             }
         }
