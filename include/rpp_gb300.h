@@ -432,7 +432,11 @@ int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream strea
  * 2D-1, and P-1 in bits 28-30 when each path's state is split over a
  * thread-block cluster of P CTAs by first letter (P divides the width; one
  * fused launch; bit 15 then puts the top level in the signature and seed
- * rows) -- tried for states whose tensor exceeds 48 KB.  A two-launch winner
+ * rows) -- tried for states whose tensor exceeds 48 KB.  In FP32, bit 16
+ * without bit 14 selects the kernels with one warp per first letter and
+ * compile-time (width, depth) (forward-only, and forward + reverse for depth
+ * >= 3), which FP32 calls of their shapes take when no schedule is recorded.
+ * A two-launch winner
  * is refined by timing other reverse sizes, then other forward sizes, and the
  * three fastest schedules with a reverse pass are timed with bit 27 too. */
 int rpp_gb_signature_tune(const rpp_gb_plan* plan, rpp_gb_stream stream, int32_t dtype,
