@@ -14,7 +14,9 @@
 //    granularity).
 //  * Each lane evaluates the Horner chains of its own coefficients from the
 //    old lower levels (letter_step): no chain arrays and no stage barriers,
-//    two __syncwarp per step.
+//    two or three __syncwarp per step.  The one exception: the two chains
+//    the top rows continue are formed once per level D-2 coefficient and
+//    shared by its W top rows through shared memory.
 //  * Width and depth are compile-time, so every stage, chain offset, level
 //    size and index split is a constant and the loops unroll.
 //  * The top level lives in registers: lane l holds the rows l, l + 32, ... of
@@ -50,7 +52,8 @@ constexpr uint32_t cpow(uint32_t w, int n) {
 // Per-warp layout (floats): two buffers of scaled increments (each padded to
 // a multiple of four floats, so the top's W letters load as float4), then the
 // slices of the levels kept in shared memory, 1..D-2 (level D-1 lives in
-// registers; at D = 2 level 1 stays in shared memory).  Each warp's region is a
+// registers; at D = 2 level 1 stays in shared memory), then (D >= 4) the two
+// top-row chains of each level D-2 coefficient.  Each warp's region is a
 // multiple of four floats, so every buffer starts on a 16-byte boundary.
 template <int W, int D>
 struct LetterLayout {
@@ -63,8 +66,12 @@ struct LetterLayout {
     static constexpr bool reg_dm1 = D >= 3;                // level D-1 in registers
     static constexpr int smem_levels = reg_dm1 ? D - 2 : D - 1;
     static constexpr uint32_t s_size = s_off(smem_levels + 1);
+    // D >= 4: the chains T^{D-1} and T^D at each level D-2 coefficient, shared
+    // by the W top rows below it (after S: [0, W^{D-3}) and [W^{D-3}, 2 W^{D-3}))
+    static constexpr bool shared_chains = D >= 4;
+    static constexpr uint32_t cb_size = shared_chains ? 2 * slice(D - 2) : 0;
     static constexpr uint32_t xcs = (W + 3) / 4 * 4;       // one increment buffer (x_a)
-    static constexpr uint32_t warp_floats = (2 * xcs + s_size + 3) / 4 * 4;
+    static constexpr uint32_t warp_floats = (2 * xcs + s_size + cb_size + 3) / 4 * 4;
     static constexpr uint32_t top_rows = slice(D - 1);                      // rows of W on top
     static constexpr int rows_per_lane = static_cast<int>((top_rows + 31) / 32);
 };
@@ -92,12 +99,15 @@ constexpr int lower_per_lane() {
 //     T_1 = S_1 + x_c / n,   T_j = S_j[a_1..a_j] + T_{j-1} x_{a_j} / (n-j+1),
 // and the new S_n is T_n (the top level adds T_{D-1} x_a to its registers).
 // These are the shared-memory kernel's chain values, formed by the same fused
-// multiply-adds in the same order, so the results are identical; only the
-// sharing of a prefix's chain value between coefficients is given up (17 %
-// more FMAs at W8 D4), for no chain arrays, no stage barriers and little
-// index arithmetic.  All lanes read the old levels before any lane writes the
-// new ones (one __syncwarp between); the caller's __syncwarp after refreshing
-// the increment orders the writes before the next step's reads.
+// multiply-adds in the same order, so the results are identical; the sharing
+// of a prefix's chain value between coefficients is given up on levels 1..D-2
+// (their chains are short), for no chain arrays, no stage barriers and little
+// index arithmetic.  The top rows' chains to level D-2 (D >= 4) are formed
+// beside the level D-2 coefficient's own and read from shared memory by its W
+// rows (one __syncwarp): recomputed per row they cost (D-3) loads, multiplies
+// and FMAs twice over.  All lanes read the old levels before any lane writes
+// the new ones (one __syncwarp between); the caller's __syncwarp after
+// refreshing the increment orders the writes before the next step's reads.
 // `with_top` false: the top rows are left alone (a gradient-only call needs
 // levels 1..D-1 only).
 template <int W, int D>
@@ -130,16 +140,30 @@ __device__ __forceinline__ void letter_step(float* S, const float* x,
             const uint32_t u = lane + 32u * q;
             if (u < sl) {
                 float acc = t1[n];
+                // on level D-2 (D >= 4) also the chains T^D and T^{D-1} of u,
+                // which the W top rows below u continue
+                constexpr bool tops = Lay::shared_chains;
+                float accd = t1[D], accm = t1[D - 1];
 #pragma unroll
                 for (int j = 2; j <= n; ++j) {
                     const uint32_t pref = u / cpow(W, n - j);  // index of (c, a_2..a_j) in level j's slice
-                    const float xm = __fmul_rn(x[pref % W], 1.0f / static_cast<float>(n - j + 1));
-                    acc = fmaf(acc, xm, S[Lay::s_off(j) + pref]);
+                    const float xp = x[pref % W];
+                    const float sj = S[Lay::s_off(j) + pref];
+                    acc = fmaf(acc, __fmul_rn(xp, 1.0f / static_cast<float>(n - j + 1)), sj);
+                    if (tops && n == NS) {
+                        accd = fmaf(accd, __fmul_rn(xp, 1.0f / static_cast<float>(D - j + 1)), sj);
+                        accm = fmaf(accm, __fmul_rn(xp, 1.0f / static_cast<float>(D - j)), sj);
+                    }
                 }
                 nv[v] = acc;
+                if (tops && n == NS) {
+                    S[Lay::s_size + u] = accm;
+                    S[Lay::s_size + sl + u] = accd;
+                }
             }
         }
     }
+    if constexpr (Lay::shared_chains) __syncwarp();  // the top rows' chains are in place
     // level D-1 in registers (lane owns coefficients lane + 32 r, which are
     // also the prefixes of its top rows) and the top rows
     float x1[W];
@@ -160,16 +184,13 @@ __device__ __forceinline__ void letter_step(float* S, const float* x,
     for (int r = 0; r < R; ++r) {
         const uint32_t row = lane + 32u * r;
         if (row < Lay::top_rows) {
-            // chains T^{D-1} (the new S_{D-1}) and T^D along the row's prefixes
+            // chains T^{D-1} (the new S_{D-1}) and T^D along the row's
+            // prefixes, to level D-2: from the level D-2 pass (D >= 4)
             float accd = t1[D];
             float accm = t1[D - 1];
-#pragma unroll
-            for (int j = 2; j < D - 1; ++j) {
-                const uint32_t pref = row / cpow(W, D - 1 - j);
-                const float sj = S[Lay::s_off(j) + pref];
-                const float xp = x[pref % W];
-                accd = fmaf(accd, __fmul_rn(xp, 1.0f / static_cast<float>(D - j + 1)), sj);
-                accm = fmaf(accm, __fmul_rn(xp, 1.0f / static_cast<float>(D - j)), sj);
+            if constexpr (Lay::shared_chains) {
+                accm = S[Lay::s_size + row / W];
+                accd = S[Lay::s_size + Lay::slice(D - 2) + row / W];
             }
             if constexpr (Lay::reg_dm1) {
                 const float xa = x[row % W];
