@@ -377,30 +377,30 @@ struct LetterRevLayout {
     }
     static constexpr int lo_total = lo(D - 1) > 0 ? lo(D - 1) : 1;
     static constexpr int pr_total = pr(D - 1) > 0 ? pr(D - 1) : 1;
+    // Family form (letter_reverse_step_family): when level D-2 of a slice has
+    // 24..32 coefficients (W5 D5: 25, W3 D6: 27), lane u < fam owns level D-2
+    // coefficient u, its W children on level D-1 and their W^2 top
+    // coefficients, so the recovery of level D-1, the top rows and the
+    // cotangent chains of level D-2 run in its registers with compile-time
+    // letters; only levels 1..D-3 go through the passes over shared memory.
+    static constexpr uint32_t fam = D >= 4 ? sl(D - 2) : 0;
+    static constexpr bool family = D >= 4 && fam >= 24 && fam <= 32;
+    static constexpr int lower = family ? D - 3 : D - 2;  // levels of the shared-memory passes
     static constexpr int steps_per_block = 8;  // letter partials reduced across warps once per block
     // per CTA after the W warp regions: [2][steps_per_block][W warps][W letters]
     static constexpr uint32_t pbuf_floats = 2u * steps_per_block * W * W;
 };
 
-// One reverse step of warp c.  `region` is the warp's shared memory, `xb` the
-// step's increment (x_a at a).  slo / glo: the lane's coefficients of S and G
-// on levels 1..D-2; pinv: its pair scales.  Adds this warp's letter terms to
-// xa.  Ends with __syncwarp.
-template <int W, int D>
-__device__ __forceinline__ void letter_reverse_step(float* region, const float* xb,
-                                                    const float (&gtop)[LetterLayout<W, D>::rows_per_lane][W],
-                                                    float (&sd)[LetterLayout<W, D>::rows_per_lane],
-                                                    float (&gd)[LetterLayout<W, D>::rows_per_lane],
-                                                    float (&slo)[LetterRevLayout<W, D>::lo_total],
-                                                    float (&glo)[LetterRevLayout<W, D>::lo_total],
-                                                    const float (&pinv)[LetterRevLayout<W, D>::pr_total],
-                                                    float (&xa)[W], uint32_t c, uint32_t lane) {
+// Recovery of levels 1..LL of warp c's slice, bottom-up, with their chains
+// (the lane's coefficients in slo).  Ends with __syncwarp.
+template <int W, int D, int LL>
+__device__ __forceinline__ void letter_recover_lower(float* region, const float* xb,
+                                                     float (&slo)[LetterRevLayout<W, D>::lo_total], uint32_t c,
+                                                     uint32_t lane) {
     using F = LetterLayout<W, D>;
     using Rev = LetterRevLayout<W, D>;
-    constexpr int R = F::rows_per_lane;
-    // recovery of levels 1..D-2, bottom-up, and their chains
 #pragma unroll
-    for (int j = 1; j <= D - 2; ++j) {
+    for (int j = 1; j <= LL; ++j) {
         const uint32_t sl = F::slice(j);
 #pragma unroll
         for (uint32_t q = 0; q < (sl + 31) / 32; ++q) {
@@ -420,48 +420,23 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
         }
         __syncwarp();
     }
-    // the top rows: recovery of level D-1 (registers), T^D_{D-1}, A^D_{D-1}
-    // and the top level's letter terms
-    float x1[W];
-    if constexpr (W % 4 == 0) {
+}
+
+// Levels LL..1: the cotangent chains of each (chain n, row p) pair from p's
+// children on level j+1 (chain n = j+1: G_{j+1} as of the step's start),
+// with the children's letter terms; then G_j += sum_{n>j} A^n_j on levels
+// 1..LL (the lane's own coefficients), the new value copied to chain n = j
+// of level j for the next step's pass over level j-1, and the letter term of
+// the word c, sum_n A^n_1 / n with A^1_1 the old G_1.  Ends with __syncwarp.
+template <int W, int D, int LL>
+__device__ __forceinline__ void letter_cotangent_lower(float* region, const float (&x1)[W],
+                                                       float (&glo)[LetterRevLayout<W, D>::lo_total],
+                                                       const float (&pinv)[LetterRevLayout<W, D>::pr_total],
+                                                       float (&xa)[W], uint32_t c, uint32_t lane) {
+    using F = LetterLayout<W, D>;
+    using Rev = LetterRevLayout<W, D>;
 #pragma unroll
-        for (int a = 0; a < W; a += 4) {
-            const float4 x4 = *reinterpret_cast<const float4*>(xb + a);
-            x1[a] = x4.x;
-            x1[a + 1] = x4.y;
-            x1[a + 2] = x4.z;
-            x1[a + 3] = x4.w;
-        }
-    } else {
-#pragma unroll
-        for (int a = 0; a < W; ++a) x1[a] = xb[a];
-    }
-#pragma unroll
-    for (int q = 0; q < R; ++q) {
-        const uint32_t p = lane + 32u * q;
-        if (p < F::top_rows) {
-            const uint32_t pu = p / W, a = p % W;
-            const float xl = xb[a];
-            const float s = fmaf(-region[Rev::tf(D - 2, D - 1) + pu], xl, sd[q]);
-            sd[q] = s;
-            const float td = fmaf(region[Rev::tf(D - 2, D) + pu], __fmul_rn(xl, 0.5f), s);
-            float acc = 0.0f;
-#pragma unroll
-            for (int e = 0; e < W; ++e) {
-                acc = fmaf(gtop[q][e], x1[e], acc);
-                xa[e] = fmaf(gtop[q][e], td, xa[e]);
-            }
-            region[Rev::ab(D - 1, D - 1) + p] = gd[q];
-            region[Rev::ab(D - 1, D) + p] = acc;
-            gd[q] += acc;
-        }
-    }
-    __syncwarp();
-    // levels D-2..1: the cotangent chains of each (chain n, row p) pair from
-    // p's children (chain n = j+1 of level j+1: G_{j+1} as of the step's
-    // start), with the children's letter terms
-#pragma unroll
-    for (int j = D - 2; j >= 1; --j) {
+    for (int j = LL; j >= 1; --j) {
         const uint32_t sl = F::slice(j);
         const uint32_t pairs = static_cast<uint32_t>(D - j) * sl;
 #pragma unroll
@@ -483,12 +458,8 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
         }
         __syncwarp();
     }
-    // G_j += sum_{n>j} A^n_j on levels 1..D-2 (the lane's own coefficients),
-    // the new value copied to chain n = j of level j for the next step's
-    // pass over level j-1; and the letter term of the word c,
-    // sum_n A^n_1 / n with A^1_1 the old G_1
 #pragma unroll
-    for (int j = 1; j <= D - 2; ++j) {
+    for (int j = 1; j <= LL; ++j) {
         const uint32_t sl = F::slice(j);
 #pragma unroll
         for (uint32_t q = 0; q < (sl + 31) / 32; ++q) {
@@ -515,88 +486,140 @@ __device__ __forceinline__ void letter_reverse_step(float* region, const float* 
     __syncwarp();
 }
 
-// Forward and reverse pass of one path by warp c (k_signature_letters_rev).
-// Modes: kForward | kBackward [| kTopLevel] (the forward pass first, writing
-// the signature row with kTopLevel) and kBackward | kLoadFinal (the final
-// signature read from sig).  `pbuf` is the CTA's partials buffer
-// (LetterRevLayout::pbuf_floats), `region` the warp's shared memory
-// (LetterRevLayout::warp_floats).  Contains CTA barriers: every warp of the
-// CTA runs the same path.
+template <int W>
+__device__ __forceinline__ void load_letters(float (&x1)[W], const float* xb) {
+    if constexpr (W % 4 == 0) {
+#pragma unroll
+        for (int a = 0; a < W; a += 4) {
+            const float4 x4 = *reinterpret_cast<const float4*>(xb + a);
+            x1[a] = x4.x;
+            x1[a + 1] = x4.y;
+            x1[a + 2] = x4.z;
+            x1[a + 3] = x4.w;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < W; ++a) x1[a] = xb[a];
+    }
+}
+
+// One reverse step of warp c, row form.  `region` is the warp's shared
+// memory, `xb` the step's increment (x_a at a).  sd / gd: levels D-1 of S and
+// G (rows lane + 32 q); slo / glo: the lane's coefficients of levels 1..D-2;
+// pinv: its pair scales.  Adds this warp's letter terms to xa.  Ends with
+// __syncwarp.
 template <int W, int D>
-__device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, int64_t b, int64_t off, int64_t len,
-                                               float* sig, int64_t sig_stride, const float* __restrict__ seed,
-                                               int64_t seed_stride, float* grad, int mode, float* region,
-                                               float* pbuf, uint32_t c, uint32_t lane) {
+__device__ __forceinline__ void letter_reverse_step(float* region, const float* xb,
+                                                    const float (&gtop)[LetterLayout<W, D>::rows_per_lane][W],
+                                                    float (&sd)[LetterLayout<W, D>::rows_per_lane],
+                                                    float (&gd)[LetterLayout<W, D>::rows_per_lane],
+                                                    float (&slo)[LetterRevLayout<W, D>::lo_total],
+                                                    float (&glo)[LetterRevLayout<W, D>::lo_total],
+                                                    const float (&pinv)[LetterRevLayout<W, D>::pr_total],
+                                                    float (&xa)[W], uint32_t c, uint32_t lane) {
     using F = LetterLayout<W, D>;
     using Rev = LetterRevLayout<W, D>;
     constexpr int R = F::rows_per_lane;
-    constexpr int NB = Rev::steps_per_block;  // steps per partials block
-    constexpr int PF = 4;                     // increments prefetched ahead = steps per loop iteration
-    float* S = region + 2 * F::xcs;
-    float sd[R];
-    float slo[Rev::lo_total], glo[Rev::lo_total];
-    if (mode & kLoadFinal) {
-        const float* src = sig + b * sig_stride;
-#pragma unroll
-        for (int j = 1; j <= D - 2; ++j)
-#pragma unroll
-            for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
-                const uint32_t u = lane + 32u * q;
-                slo[Rev::lo(j) + q] = u < F::slice(j) ? src[level_start<W>(j) + c * F::slice(j) + u] : 0.0f;
-            }
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const uint32_t p = lane + 32u * q;
-            sd[q] = p < F::top_rows ? src[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
-        }
-    } else {
-        float top[R][W];
-        const bool with_top = mode & kTopLevel;
-        letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, with_top);
-        if (with_top && sig) letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
-#pragma unroll
-        for (int j = 1; j <= D - 2; ++j)
-#pragma unroll
-            for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
-                const uint32_t u = lane + 32u * q;
-                slo[Rev::lo(j) + q] = u < F::slice(j) ? S[F::s_off(j) + u] : 0.0f;
-            }
-    }
-    // the seed: top rows, level D-1 and the lane's lower coefficients
-    const float* sdr = seed + b * seed_stride;
-    float gtop[R][W], gd[R];
-#pragma unroll
-    for (int j = 1; j <= D - 2; ++j)
-#pragma unroll
-        for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
-            const uint32_t u = lane + 32u * q;
-            glo[Rev::lo(j) + q] = u < F::slice(j) ? sdr[level_start<W>(j) + c * F::slice(j) + u] : 0.0f;
-        }
+    letter_recover_lower<W, D, D - 2>(region, xb, slo, c, lane);
+    // the top rows: recovery of level D-1 (registers), T^D_{D-1}, A^D_{D-1}
+    // and the top level's letter terms
+    float x1[W];
+    load_letters<W>(x1, xb);
 #pragma unroll
     for (int q = 0; q < R; ++q) {
         const uint32_t p = lane + 32u * q;
-        const bool row = p < F::top_rows;
-        gd[q] = row ? sdr[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
+        if (p < F::top_rows) {
+            const uint32_t pu = p / W, a = p % W;
+            const float xl = xb[a];
+            const float s = fmaf(-region[Rev::tf(D - 2, D - 1) + pu], xl, sd[q]);
+            sd[q] = s;
+            const float td = fmaf(region[Rev::tf(D - 2, D) + pu], __fmul_rn(xl, 0.5f), s);
+            float acc = 0.0f;
 #pragma unroll
-        for (int a = 0; a < W; ++a) gtop[q][a] = row ? sdr[level_start<W>(D) + c * F::slice(D) + p * W + a] : 0.0f;
-    }
-    // chain n = j of each level j <= D-2: G_j as of the first step's start
-#pragma unroll
-    for (int j = 1; j <= D - 2; ++j)
-#pragma unroll
-        for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
-            const uint32_t u = lane + 32u * q;
-            if (u < F::slice(j)) region[Rev::ab(j, j) + u] = glo[Rev::lo(j) + q];
+            for (int e = 0; e < W; ++e) {
+                acc = fmaf(gtop[q][e], x1[e], acc);
+                xa[e] = fmaf(gtop[q][e], td, xa[e]);
+            }
+            region[Rev::ab(D - 1, D - 1) + p] = gd[q];
+            region[Rev::ab(D - 1, D) + p] = acc;
+            gd[q] += acc;
         }
-    // the scale 1 / (n - j) of each (chain n, row) pair of level j this lane
-    // takes: pair e = lane + 32 q, n - j = e / W^{j-1} + 1
-    float pinv[Rev::pr_total];
+    }
+    __syncwarp();
+    letter_cotangent_lower<W, D, D - 2>(region, x1, glo, pinv, xa, c, lane);
+}
+
+// One reverse step of warp c, family form (LetterRevLayout::family): lane
+// u < fam holds level D-2 coefficient u of S and G (sf, gf), its children's
+// level D-1 coefficients (sdf, gdf) and their top rows (gtop[a][b] = G'_D at
+// (u, a, b)).  The family pass recovers u and its children, forms the top
+// level's letter terms and A^D_{D-1} of each child, the children's letter
+// terms on level D-1 and A^{D-1}_{D-2}, A^D_{D-2} of u -- the sums the row
+// form spreads over its top pass and a pass over level D-2's pairs.  Ends
+// with __syncwarp.
+template <int W, int D>
+__device__ __forceinline__ void letter_reverse_step_family(float* region, const float* xb, const float (&gtop)[W][W],
+                                                           float (&sdf)[W], float (&gdf)[W], float& sf, float& gf,
+                                                           float (&slo)[LetterRevLayout<W, D>::lo_total],
+                                                           float (&glo)[LetterRevLayout<W, D>::lo_total],
+                                                           const float (&pinv)[LetterRevLayout<W, D>::pr_total],
+                                                           float (&xa)[W], uint32_t c, uint32_t lane) {
+    using Rev = LetterRevLayout<W, D>;
+    static_assert(Rev::family, "family form");
+    letter_recover_lower<W, D, D - 3>(region, xb, slo, c, lane);
+    float x1[W];
+    load_letters<W>(x1, xb);
+    if (lane < Rev::fam) {
+        const uint32_t u = lane, pu = u / W;
+        const float xv = xb[u % W];
+        // recovery of u and its chains T^{D-1}_{D-2}, T^D_{D-2}
+        const float s = fmaf(-region[Rev::tf(D - 3, D - 2) + pu], xv, sf);
+        sf = s;
+        const float tm = fmaf(region[Rev::tf(D - 3, D - 1) + pu], __fmul_rn(xv, 0.5f), s);
+        const float td = fmaf(region[Rev::tf(D - 3, D) + pu], __fmul_rn(xv, 1.0f / 3.0f), s);
+        const float td2 = __fmul_rn(td, 0.5f);  // T^D_{D-2}[u] / 2
+        float am = 0.0f, ad = 0.0f;             // A^{D-1}_{D-2}[u], A^D_{D-2}[u]
 #pragma unroll
-    for (int j = 1; j <= D - 2; ++j)
+        for (int a = 0; a < W; ++a) {
+            const float xh = __fmul_rn(x1[a], 0.5f);
+            const float s4 = fmaf(-tm, x1[a], sdf[a]);  // S^-_{D-1}[u a]
+            sdf[a] = s4;
+            const float t4 = fmaf(td, xh, s4);  // T^D_{D-1}[u a]
+            float acc = 0.0f;                   // A^D_{D-1}[u a]
 #pragma unroll
-        for (uint32_t q = 0; q < ((D - j) * F::slice(j) + 31) / 32; ++q)
-            pinv[Rev::pr(j) + q] = 1.0f / static_cast<float>((lane + 32u * q) / F::slice(j) + 1);
-    // increments from the last: lane a < W loads letter a PF steps ahead
+            for (int e = 0; e < W; ++e) {
+                acc = fmaf(gtop[a][e], x1[e], acc);
+                xa[e] = fmaf(gtop[a][e], t4, xa[e]);
+            }
+            const float go = gdf[a];  // A^{D-1}_{D-1}[u a]: the old G_{D-1}
+            gdf[a] = go + acc;
+            xa[a] = fmaf(go, tm, xa[a]);
+            xa[a] = fmaf(acc, td2, xa[a]);
+            am = fmaf(go, x1[a], am);
+            ad = fmaf(acc, xh, ad);
+        }
+        region[Rev::ab(D - 2, D - 2) + u] = gf;
+        region[Rev::ab(D - 2, D - 1) + u] = am;
+        region[Rev::ab(D - 2, D) + u] = ad;
+        gf = gf + am + ad;
+    }
+    __syncwarp();
+    letter_cotangent_lower<W, D, D - 3>(region, x1, glo, pinv, xa, c, lane);
+}
+
+// The reverse loop of one path by warp c: increments from the last (lane
+// a < W loads letter a four steps ahead), `step(xb, xa)` per increment, the
+// warp's letter partials per step into pbuf, and once per 8 steps (and at
+// the end) one CTA barrier after which threads t < 8 W add the W warps'
+// partials in warp order into the gradient rows.
+template <int W, int D, typename Step>
+__device__ __forceinline__ void letter_reverse_loop(const float* __restrict__ incr, int64_t off, int64_t len,
+                                                    float* grad, float* region, float* pbuf, uint32_t c,
+                                                    uint32_t lane, Step&& step) {
+    using F = LetterLayout<W, D>;
+    using Rev = LetterRevLayout<W, D>;
+    constexpr int NB = Rev::steps_per_block;  // steps per partials block
+    constexpr int PF = 4;                     // increments prefetched ahead = steps per loop iteration
     const bool xlane = lane < static_cast<uint32_t>(W);
     const float* xin = incr + off * W;
     float* xbuf = region + Rev::xb_off;
@@ -618,11 +641,11 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
             // ring slot q held increment i (now in the buffer): refill it
             // with increment i + PF
             if (xlane && i + PF < len) xr[q] = __ldg(xin + (len - 1 - i - PF) * W + lane);
-            letter_reverse_step<W, D>(region, xbuf + (i & 1) * F::xcs, gtop, sd, gd, slo, glo, pinv, xa, c, lane);
+            step(xbuf + (i & 1) * F::xcs, xa);
             if (xlane && i + 1 < len) xbuf[((i + 1) & 1) * F::xcs + lane] = xr[(q + 1) % PF];
             const uint32_t slot = static_cast<uint32_t>(i % NB);
             float* pb = pbuf + ((i / NB) & 1) * (NB * W * W);
-            // this warp's letter partials: pb[q][c][a]
+            // this warp's letter partials: pb[slot][c][a]
             uint32_t base = 0, cnt = W;
             letter_butterfly<float, W>(xa, lane, 16u, base, cnt);
             if (cnt > 0u && (lane & ((32u >> halvings) - 1u)) == 0u) pb[(slot * W + c) * W + base] = xa[0];
@@ -643,6 +666,105 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
                 }
             }
         }
+    }
+}
+
+// Forward and reverse pass of one path by warp c (k_signature_letters_rev).
+// Modes: kForward | kBackward [| kTopLevel] (the forward pass first, writing
+// the signature row with kTopLevel) and kBackward | kLoadFinal (the final
+// signature read from sig).  `pbuf` is the CTA's partials buffer
+// (LetterRevLayout::pbuf_floats), `region` the warp's shared memory
+// (LetterRevLayout::warp_floats).  Contains CTA barriers: every warp of the
+// CTA runs the same path.
+template <int W, int D>
+__device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, int64_t b, int64_t off, int64_t len,
+                                               float* sig, int64_t sig_stride, const float* __restrict__ seed,
+                                               int64_t seed_stride, float* grad, int mode, float* region,
+                                               float* pbuf, uint32_t c, uint32_t lane) {
+    using F = LetterLayout<W, D>;
+    using Rev = LetterRevLayout<W, D>;
+    constexpr int R = F::rows_per_lane;
+    constexpr int LL = Rev::lower;
+    float* S = region + 2 * F::xcs;
+    const float* src = sig + b * sig_stride;
+    const float* sdr = seed + b * seed_stride;
+    // the final state: levels 1..LL to the owner lanes' registers (slo), the
+    // rest (level D-1, and in the family form level D-2) kept by the form below
+    float sd[R];
+    float slo[Rev::lo_total], glo[Rev::lo_total];
+    if (mode & kLoadFinal) {
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const uint32_t p = lane + 32u * q;
+            sd[q] = p < F::top_rows ? src[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
+        }
+    } else {
+        float top[R][W];
+        const bool with_top = mode & kTopLevel;
+        letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, with_top);
+        if (with_top && sig) letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
+    }
+    const bool load = mode & kLoadFinal;
+#pragma unroll
+    for (int j = 1; j <= LL; ++j)
+#pragma unroll
+        for (uint32_t q = 0; q < (F::slice(j) + 31) / 32; ++q) {
+            const uint32_t u = lane + 32u * q;
+            const bool own = u < F::slice(j);
+            slo[Rev::lo(j) + q] = !own ? 0.0f : load ? src[level_start<W>(j) + c * F::slice(j) + u] : S[F::s_off(j) + u];
+            glo[Rev::lo(j) + q] = own ? sdr[level_start<W>(j) + c * F::slice(j) + u] : 0.0f;
+            // chain n = j of level j: G_j as of the first step's start
+            if (own) region[Rev::ab(j, j) + u] = glo[Rev::lo(j) + q];
+        }
+    // the scale 1 / (n - j) of each (chain n, row) pair of level j this lane
+    // takes: pair e = lane + 32 q, n - j = e / W^{j-1} + 1
+    float pinv[Rev::pr_total];
+#pragma unroll
+    for (int j = 1; j <= LL; ++j)
+#pragma unroll
+        for (uint32_t q = 0; q < ((D - j) * F::slice(j) + 31) / 32; ++q)
+            pinv[Rev::pr(j) + q] = 1.0f / static_cast<float>((lane + 32u * q) / F::slice(j) + 1);
+    if constexpr (Rev::family) {
+        // level D-1 from the row layout (lane l: rows l, l + 32, ...) to the
+        // family layout (lane u: rows u W .. u W + W-1) through the unused
+        // chain arrays of level D-1
+        float* tmp = region + Rev::ab(D - 1, D - 1);
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const uint32_t p = lane + 32u * q;
+            if (p < F::top_rows) tmp[p] = sd[q];
+        }
+        __syncwarp();
+        const uint32_t u = lane;
+        const bool fl = u < Rev::fam;
+        float sdf[W], gdf[W], gtop[W][W];
+#pragma unroll
+        for (int a = 0; a < W; ++a) {
+            sdf[a] = fl ? tmp[u * W + a] : 0.0f;
+            gdf[a] = fl ? sdr[level_start<W>(D - 1) + c * F::slice(D - 1) + u * W + a] : 0.0f;
+#pragma unroll
+            for (int e = 0; e < W; ++e)
+                gtop[a][e] = fl ? sdr[level_start<W>(D) + c * F::slice(D) + (u * W + a) * W + e] : 0.0f;
+        }
+        float sf = !fl ? 0.0f : load ? src[level_start<W>(D - 2) + c * F::slice(D - 2) + u] : S[F::s_off(D - 2) + u];
+        float gf = fl ? sdr[level_start<W>(D - 2) + c * F::slice(D - 2) + u] : 0.0f;
+        letter_reverse_loop<W, D>(incr, off, len, grad, region, pbuf, c, lane, [&](const float* xb, float(&xa)[W]) {
+            letter_reverse_step_family<W, D>(region, xb, gtop, sdf, gdf, sf, gf, slo, glo, pinv, xa, c, lane);
+        });
+    } else {
+        float gtop[R][W], gd[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const uint32_t p = lane + 32u * q;
+            const bool row = p < F::top_rows;
+            gd[q] = row ? sdr[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
+#pragma unroll
+            for (int a = 0; a < W; ++a)
+                gtop[q][a] = row ? sdr[level_start<W>(D) + c * F::slice(D) + p * W + a] : 0.0f;
+        }
+        letter_reverse_loop<W, D>(incr, off, len, grad, region, pbuf, c, lane, [&](const float* xb, float(&xa)[W]) {
+            letter_reverse_step<W, D>(region, xb, gtop, sd, gd, slo, glo, pinv, xa, c, lane);
+        });
     }
 }
 
