@@ -64,11 +64,19 @@ struct LetterLayout {
         return o;
     }
     static constexpr bool reg_dm1 = D >= 3;                // level D-1 in registers
-    static constexpr int smem_levels = reg_dm1 ? D - 2 : D - 1;
+    // Family form (letter_step_family): when level D-2 of a slice has 24..32
+    // coefficients (W5 D5: 25, W3 D6: 27), lane u < fam holds level D-2
+    // coefficient u, its W children on level D-1 and their W^2 top
+    // coefficients in registers, so their chains are formed once per lane
+    // with compile-time letters; levels 1..D-3 stay in shared memory.
+    static constexpr uint32_t fam = D >= 4 ? slice(D - 2) : 0;
+    static constexpr bool family = D >= 4 && fam >= 24 && fam <= 32;
+    static constexpr int smem_levels = family ? D - 3 : reg_dm1 ? D - 2 : D - 1;
     static constexpr uint32_t s_size = s_off(smem_levels + 1);
-    // D >= 4: the chains T^{D-1} and T^D at each level D-2 coefficient, shared
-    // by the W top rows below it (after S: [0, W^{D-3}) and [W^{D-3}, 2 W^{D-3}))
-    static constexpr bool shared_chains = D >= 4;
+    // D >= 4, row form: the chains T^{D-1} and T^D at each level D-2
+    // coefficient, shared by the W top rows below it (after S: [0, W^{D-3})
+    // and [W^{D-3}, 2 W^{D-3}))
+    static constexpr bool shared_chains = D >= 4 && !family;
     static constexpr uint32_t cb_size = shared_chains ? 2 * slice(D - 2) : 0;
     static constexpr uint32_t xcs = (W + 3) / 4 * 4;       // one increment buffer (x_a)
     static constexpr uint32_t warp_floats = (2 * xcs + s_size + cb_size + 3) / 4 * 4;
@@ -91,6 +99,25 @@ constexpr int lower_per_lane() {
     int t = 0;
     for (int n = 1; n <= LetterLayout<W, D>::smem_levels; ++n) t += static_cast<int>((cpow(W, n - 1) + 31) / 32);
     return t;
+}
+
+// The W letters of an increment buffer into registers (16-byte loads when W
+// is a multiple of 4; the buffers are 16-byte aligned).
+template <int W>
+__device__ __forceinline__ void load_letters(float (&x1)[W], const float* xb) {
+    if constexpr (W % 4 == 0) {
+#pragma unroll
+        for (int a = 0; a < W; a += 4) {
+            const float4 x4 = *reinterpret_cast<const float4*>(xb + a);
+            x1[a] = x4.x;
+            x1[a + 1] = x4.y;
+            x1[a + 2] = x4.z;
+            x1[a + 3] = x4.w;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < W; ++a) x1[a] = xb[a];
+    }
 }
 
 // One forward step of warp c (its first-letter slice).  Every coefficient's
@@ -218,33 +245,98 @@ __device__ __forceinline__ void letter_step(float* S, const float* x,
     }
 }
 
-// The forward pass of one path with increments [off, off + len) by warp c of
-// the path's W warps (its first-letter slice): leaves levels 1..smem_levels
-// of the slice in S, level D-1 in sd and, with `with_top`, the top rows in
-// `top`.  `xcb` holds the two increment buffers (2 xcs floats).  Warps never
-// wait on each other; ends with __syncwarp.
+// One forward step of warp c, family form (LetterLayout::family): levels
+// 1..D-3 as in letter_step; lane u < fam forms the chains of its level D-2
+// coefficient u along u's prefixes (to T^{D-2}, the new S_{D-2}[u], and the
+// chains T^{D-1}, T^D its children continue), then its W children on level
+// D-1 and their top rows with compile-time letters.  The same fused
+// multiply-adds in the same order as letter_step, so the results are
+// identical.
 template <int W, int D>
-__device__ __forceinline__ void letter_forward(const float* __restrict__ incr, int64_t off, int64_t len, float* xcb,
-                                               float* S, float (&top)[LetterLayout<W, D>::rows_per_lane][W],
-                                               float (&sd)[LetterLayout<W, D>::rows_per_lane], uint32_t c,
-                                               uint32_t lane, bool with_top) {
+__device__ __forceinline__ void letter_step_family(float* S, const float* x, float (&top)[W][W], float (&sdf)[W],
+                                                   float& sf, uint32_t c, uint32_t lane, bool with_top) {
     using Lay = LetterLayout<W, D>;
-    static_assert(D >= 2 && W <= 32, "one letter per lane");
-    static_assert(LetterLayout<W, D>::rows_per_lane * W <= 32, "at most 32 registers of top-level rows");
-    constexpr int R = Lay::rows_per_lane;
+    constexpr int NS = Lay::smem_levels;  // D - 3 >= 1
+    const float s1 = S[Lay::s_off(1)];
+    const float xcc = x[c];
+    float t1[D + 1];  // T^n_1 = S_1 + S_0 x_c / n (S_0 = 1)
+#pragma unroll
+    for (int n = 2; n <= D; ++n) t1[n] = s1 + __fmul_rn(xcc, 1.0f / static_cast<float>(n));
+    float nv[lower_per_lane<W, D>() > 0 ? lower_per_lane<W, D>() : 1];
+    int v = 0;
+    nv[v++] = s1 + xcc;
+#pragma unroll
+    for (int n = 2; n <= NS; ++n) {
+        const uint32_t sl = Lay::slice(n);
+#pragma unroll
+        for (uint32_t q = 0; q < (sl + 31) / 32; ++q, ++v) {
+            const uint32_t u = lane + 32u * q;
+            if (u < sl) {
+                float acc = t1[n];
+#pragma unroll
+                for (int j = 2; j <= n; ++j) {
+                    const uint32_t pref = u / cpow(W, n - j);
+                    acc = fmaf(acc, __fmul_rn(x[pref % W], 1.0f / static_cast<float>(n - j + 1)),
+                               S[Lay::s_off(j) + pref]);
+                }
+                nv[v] = acc;
+            }
+        }
+    }
+    float x1[W];
+    load_letters<W>(x1, x);
+    if (lane < Lay::fam) {
+        const uint32_t u = lane;
+        float acc = t1[D - 2], accm = t1[D - 1], accd = t1[D];
+#pragma unroll
+        for (int j = 2; j <= D - 2; ++j) {
+            const uint32_t pref = u / cpow(W, D - 2 - j);
+            const float xp = x[pref % W];
+            const float sj = j == D - 2 ? sf : S[Lay::s_off(j) + pref];
+            acc = fmaf(acc, __fmul_rn(xp, 1.0f / static_cast<float>(D - 2 - j + 1)), sj);
+            accd = fmaf(accd, __fmul_rn(xp, 1.0f / static_cast<float>(D - j + 1)), sj);
+            accm = fmaf(accm, __fmul_rn(xp, 1.0f / static_cast<float>(D - j)), sj);
+        }
+        sf = acc;
+#pragma unroll
+        for (int a = 0; a < W; ++a) {
+            const float ad = fmaf(accd, __fmul_rn(x1[a], 0.5f), sdf[a]);  // T^D_{D-1}: old S_{D-1}
+            sdf[a] = fmaf(accm, x1[a], sdf[a]);                            // new S_{D-1}
+            if (with_top) {
+#pragma unroll
+                for (int e = 0; e < W; ++e) top[a][e] = fmaf(ad, x1[e], top[a][e]);
+            }
+        }
+    }
+    __syncwarp();  // every lane has read the old levels
+    v = 0;
+    if (lane == 0) S[Lay::s_off(1)] = nv[0];
+    ++v;
+#pragma unroll
+    for (int n = 2; n <= NS; ++n) {
+        const uint32_t sl = Lay::slice(n);
+#pragma unroll
+        for (uint32_t q = 0; q < (sl + 31) / 32; ++q, ++v) {
+            const uint32_t u = lane + 32u * q;
+            if (u < sl) S[Lay::s_off(n) + u] = nv[v];
+        }
+    }
+}
+
+// The increment loop of one path's forward pass by one warp: lane a < W
+// loads letter a eight steps ahead into a register ring (a step here is
+// short, and a load one step ahead left the L2 latency exposed); `step(x)`
+// runs each step on the increment buffer x (two buffers by step parity in
+// xcb).  Ends with __syncwarp.
+template <int W, int D, typename Step>
+__device__ __forceinline__ void letter_forward_loop(const float* __restrict__ incr, int64_t off, int64_t len,
+                                                    float* xcb, uint32_t lane, Step&& step) {
+    using Lay = LetterLayout<W, D>;
     constexpr int PF = 8;  // increments prefetched ahead
     const bool xlane = lane < static_cast<uint32_t>(W);  // lane a < W holds letter a
     const float* xin = incr + off * W;
-    for (uint32_t i = lane; i < Lay::s_size; i += 32) S[i] = 0.0f;
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-        sd[i] = 0.0f;
-#pragma unroll
-        for (int a = 0; a < W; ++a) top[i][a] = 0.0f;
-    }
-    // prefetch ring: xr[q] holds this lane's letter of increment k0 + q for
-    // the block of PF steps starting at k0 (loads issued PF steps ahead, so
-    // their L2 latency is hidden behind PF short steps)
+    // xr[q] holds this lane's letter of increment k0 + q for the block of PF
+    // steps starting at k0
     float xr[PF];
 #pragma unroll
     for (int q = 0; q < PF; ++q) xr[q] = (xlane && q < len) ? __ldg(xin + q * W + lane) : 0.0f;
@@ -258,11 +350,58 @@ __device__ __forceinline__ void letter_forward(const float* __restrict__ incr, i
             // slot q has been consumed (x_k is in the increment buffer):
             // refill it with x_{k+PF}
             if (xlane && k + PF < len) xr[q] = __ldg(xin + (k + PF) * W + lane);
-            letter_step<W, D>(S, xcb + (k & 1) * Lay::xcs, top, sd, c, lane, with_top);
+            step(xcb + (k & 1) * Lay::xcs);
             if (xlane && k + 1 < len) xcb[((k + 1) & 1) * Lay::xcs + lane] = xr[(q + 1) % PF];
             __syncwarp();
         }
     }
+}
+
+// The forward pass of one path with increments [off, off + len) by warp c of
+// the path's W warps (its first-letter slice), row form: leaves levels
+// 1..smem_levels of the slice in S, level D-1 in sd and, with `with_top`, the
+// top rows in `top`.  `xcb` holds the two increment buffers (2 xcs floats).
+// Warps never wait on each other; ends with __syncwarp.
+template <int W, int D>
+__device__ __forceinline__ void letter_forward(const float* __restrict__ incr, int64_t off, int64_t len, float* xcb,
+                                               float* S, float (&top)[LetterLayout<W, D>::rows_per_lane][W],
+                                               float (&sd)[LetterLayout<W, D>::rows_per_lane], uint32_t c,
+                                               uint32_t lane, bool with_top) {
+    using Lay = LetterLayout<W, D>;
+    static_assert(D >= 2 && W <= 32, "one letter per lane");
+    static_assert(LetterLayout<W, D>::rows_per_lane * W <= 32, "at most 32 registers of top-level rows");
+    constexpr int R = Lay::rows_per_lane;
+    for (uint32_t i = lane; i < Lay::s_size; i += 32) S[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        sd[i] = 0.0f;
+#pragma unroll
+        for (int a = 0; a < W; ++a) top[i][a] = 0.0f;
+    }
+    letter_forward_loop<W, D>(incr, off, len, xcb, lane,
+                              [&](const float* x) { letter_step<W, D>(S, x, top, sd, c, lane, with_top); });
+}
+
+// The same, family form (LetterLayout::family): lane u < fam ends with level
+// D-2 coefficient u in sf, its children's level D-1 coefficients in sdf and,
+// with `with_top`, their top rows in `top`.
+template <int W, int D>
+__device__ __forceinline__ void letter_forward_family(const float* __restrict__ incr, int64_t off, int64_t len,
+                                                      float* xcb, float* S, float (&top)[W][W], float (&sdf)[W],
+                                                      float& sf, uint32_t c, uint32_t lane, bool with_top) {
+    using Lay = LetterLayout<W, D>;
+    static_assert(Lay::family, "family form");
+    for (uint32_t i = lane; i < Lay::s_size; i += 32) S[i] = 0.0f;
+    sf = 0.0f;
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+        sdf[i] = 0.0f;
+#pragma unroll
+        for (int a = 0; a < W; ++a) top[i][a] = 0.0f;
+    }
+    letter_forward_loop<W, D>(incr, off, len, xcb, lane, [&](const float* x) {
+        letter_step_family<W, D>(S, x, top, sdf, sf, c, lane, with_top);
+    });
 }
 
 // Warp c's part of the signature row dst: S_0 (warp 0), the slices of levels
@@ -293,6 +432,32 @@ __device__ __forceinline__ void letter_store(float* dst, const float* S,
     }
 }
 
+// The same, family form: levels 1..D-3 from S, then lane u < fam's level D-2
+// coefficient, its children's level D-1 coefficients and their top rows.
+template <int W, int D>
+__device__ __forceinline__ void letter_store_family(float* dst, const float* S, const float (&top)[W][W],
+                                                    const float (&sdf)[W], float sf, uint32_t c, uint32_t lane) {
+    using Lay = LetterLayout<W, D>;
+    if (c == 0 && lane == 0) dst[0] = 1.0f;
+#pragma unroll
+    for (int j = 1; j <= Lay::smem_levels; ++j) {
+        const uint32_t sl = Lay::slice(j);
+        for (uint32_t u = lane; u < sl; u += 32) dst[level_start<W>(j) + c * sl + u] = S[Lay::s_off(j) + u];
+    }
+    if (lane < Lay::fam) {
+        const uint32_t u = lane;
+        dst[level_start<W>(D - 2) + c * Lay::slice(D - 2) + u] = sf;
+        float* ddm1 = dst + level_start<W>(D - 1) + c * Lay::slice(D - 1) + u * W;
+        float* dtop = dst + level_start<W>(D) + c * Lay::slice(D) + u * W * W;
+#pragma unroll
+        for (int a = 0; a < W; ++a) {
+            ddm1[a] = sdf[a];
+#pragma unroll
+            for (int e = 0; e < W; ++e) dtop[a * W + e] = top[a][e];
+        }
+    }
+}
+
 // One path b with increments [off, off + len) by warp c of the path's W
 // warps, into the signature row sig + b*sig_stride.  `region` is the warp's
 // shared memory (LetterLayout::warp_floats floats: two increment buffers,
@@ -302,12 +467,18 @@ __device__ __forceinline__ void letter_path(const float* __restrict__ incr, int6
                                             float* sig, int64_t sig_stride, float* region, uint32_t c,
                                             uint32_t lane) {
     using Lay = LetterLayout<W, D>;
-    constexpr int R = Lay::rows_per_lane;
-    float top[R][W];
-    float sd[R];
     float* S = region + 2 * Lay::xcs;
-    letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, true);
-    letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
+    if constexpr (Lay::family) {
+        float top[W][W], sdf[W], sf;
+        letter_forward_family<W, D>(incr, off, len, region, S, top, sdf, sf, c, lane, true);
+        letter_store_family<W, D>(sig + b * sig_stride, S, top, sdf, sf, c, lane);
+    } else {
+        constexpr int R = Lay::rows_per_lane;
+        float top[R][W];
+        float sd[R];
+        letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, true);
+        letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
+    }
     __syncwarp();
 }
 
@@ -383,8 +554,8 @@ struct LetterRevLayout {
     // coefficients, so the recovery of level D-1, the top rows and the
     // cotangent chains of level D-2 run in its registers with compile-time
     // letters; only levels 1..D-3 go through the passes over shared memory.
-    static constexpr uint32_t fam = D >= 4 ? sl(D - 2) : 0;
-    static constexpr bool family = D >= 4 && fam >= 24 && fam <= 32;
+    static constexpr uint32_t fam = F::fam;
+    static constexpr bool family = F::family;
     static constexpr int lower = family ? D - 3 : D - 2;  // levels of the shared-memory passes
     static constexpr int steps_per_block = 8;  // letter partials reduced across warps once per block
     // per CTA after the W warp regions: [2][steps_per_block][W warps][W letters]
@@ -486,22 +657,6 @@ __device__ __forceinline__ void letter_cotangent_lower(float* region, const floa
     __syncwarp();
 }
 
-template <int W>
-__device__ __forceinline__ void load_letters(float (&x1)[W], const float* xb) {
-    if constexpr (W % 4 == 0) {
-#pragma unroll
-        for (int a = 0; a < W; a += 4) {
-            const float4 x4 = *reinterpret_cast<const float4*>(xb + a);
-            x1[a] = x4.x;
-            x1[a + 1] = x4.y;
-            x1[a + 2] = x4.z;
-            x1[a + 3] = x4.w;
-        }
-    } else {
-#pragma unroll
-        for (int a = 0; a < W; ++a) x1[a] = xb[a];
-    }
-}
 
 // One reverse step of warp c, row form.  `region` is the warp's shared
 // memory, `xb` the step's increment (x_a at a).  sd / gd: levels D-1 of S and
@@ -688,23 +843,38 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
     float* S = region + 2 * F::xcs;
     const float* src = sig + b * sig_stride;
     const float* sdr = seed + b * seed_stride;
-    // the final state: levels 1..LL to the owner lanes' registers (slo), the
-    // rest (level D-1, and in the family form level D-2) kept by the form below
-    float sd[R];
-    float slo[Rev::lo_total], glo[Rev::lo_total];
-    if (mode & kLoadFinal) {
+    const bool load = mode & kLoadFinal;
+    const bool with_top = mode & kTopLevel;
+    // the final state: level D-1 (and in the family form level D-2) in the
+    // form's registers, levels 1..LL in S (forward pass) or from sig
+    float sd[F::family ? 1 : R];
+    float sdf[F::family ? W : 1], sf = 0.0f;
+    if constexpr (F::family) {
+        const bool fl = lane < Rev::fam;
+        const uint32_t u = lane;
+        if (load) {
 #pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const uint32_t p = lane + 32u * q;
-            sd[q] = p < F::top_rows ? src[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
+            for (int a = 0; a < W; ++a) sdf[a] = fl ? src[level_start<W>(D - 1) + c * F::slice(D - 1) + u * W + a] : 0.0f;
+            sf = fl ? src[level_start<W>(D - 2) + c * F::slice(D - 2) + u] : 0.0f;
+        } else {
+            float top[W][W];
+            letter_forward_family<W, D>(incr, off, len, region, S, top, sdf, sf, c, lane, with_top);
+            if (with_top && sig) letter_store_family<W, D>(sig + b * sig_stride, S, top, sdf, sf, c, lane);
         }
     } else {
-        float top[R][W];
-        const bool with_top = mode & kTopLevel;
-        letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, with_top);
-        if (with_top && sig) letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
+        if (load) {
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                const uint32_t p = lane + 32u * q;
+                sd[q] = p < F::top_rows ? src[level_start<W>(D - 1) + c * F::slice(D - 1) + p] : 0.0f;
+            }
+        } else {
+            float top[R][W];
+            letter_forward<W, D>(incr, off, len, region, S, top, sd, c, lane, with_top);
+            if (with_top && sig) letter_store<W, D>(sig + b * sig_stride, S, top, sd, c, lane);
+        }
     }
-    const bool load = mode & kLoadFinal;
+    float slo[Rev::lo_total], glo[Rev::lo_total];
 #pragma unroll
     for (int j = 1; j <= LL; ++j)
 #pragma unroll
@@ -725,28 +895,16 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
         for (uint32_t q = 0; q < ((D - j) * F::slice(j) + 31) / 32; ++q)
             pinv[Rev::pr(j) + q] = 1.0f / static_cast<float>((lane + 32u * q) / F::slice(j) + 1);
     if constexpr (Rev::family) {
-        // level D-1 from the row layout (lane l: rows l, l + 32, ...) to the
-        // family layout (lane u: rows u W .. u W + W-1) through the unused
-        // chain arrays of level D-1
-        float* tmp = region + Rev::ab(D - 1, D - 1);
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const uint32_t p = lane + 32u * q;
-            if (p < F::top_rows) tmp[p] = sd[q];
-        }
-        __syncwarp();
         const uint32_t u = lane;
         const bool fl = u < Rev::fam;
-        float sdf[W], gdf[W], gtop[W][W];
+        float gdf[W], gtop[W][W];
 #pragma unroll
         for (int a = 0; a < W; ++a) {
-            sdf[a] = fl ? tmp[u * W + a] : 0.0f;
             gdf[a] = fl ? sdr[level_start<W>(D - 1) + c * F::slice(D - 1) + u * W + a] : 0.0f;
 #pragma unroll
             for (int e = 0; e < W; ++e)
                 gtop[a][e] = fl ? sdr[level_start<W>(D) + c * F::slice(D) + (u * W + a) * W + e] : 0.0f;
         }
-        float sf = !fl ? 0.0f : load ? src[level_start<W>(D - 2) + c * F::slice(D - 2) + u] : S[F::s_off(D - 2) + u];
         float gf = fl ? sdr[level_start<W>(D - 2) + c * F::slice(D - 2) + u] : 0.0f;
         letter_reverse_loop<W, D>(incr, off, len, grad, region, pbuf, c, lane, [&](const float* xb, float(&xa)[W]) {
             letter_reverse_step_family<W, D>(region, xb, gtop, sdf, gdf, sf, gf, slo, glo, pinv, xa, c, lane);
