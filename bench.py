@@ -341,16 +341,16 @@ def workload_ft_mul(pkg, torch, args, peak):
                  "eager_ms_per_launch": ms_eager})
 
 
-def workload_logsig(pkg, torch, args, peak):
-    """Log-signatures, W5 D5, 4096 paths of 256 steps: the signature launch(es)
-    and the fused log-to-Lie epilogue (ft_log + tensor_to_lie in one kernel,
-    829 Lie coefficients, nnz 10 517); the unfused ft_log and tensor_to_lie
-    launches are timed beside it."""
-    W, D, B, L = 5, 5, 4096, 256
+def workload_logsig(pkg, torch, args, peak, W=5, D=5, B=4096, L=256, seed=3):
+    """Log-signatures of B paths of L steps (W5 D5, 4096 x 256: 829 Lie
+    coefficients, nnz 10 517; the large mixed shapes W2 D12 and W16 D3, 16 384
+    x 64): the signature launch(es) under the tuner's forward-only schedule and
+    the fused log-to-Lie epilogue (ft_log + tensor_to_lie in one kernel); the
+    unfused ft_log and tensor_to_lie launches are timed beside it."""
     basis, lbasis = pkg.TensorBasis(W, D), pkg.LieBasis(W, D)
     dim, ts = basis.size(), lbasis.true_size()
     st = pkg.GB300Strategy(torch.float64)
-    g = torch.Generator(device="cuda").manual_seed(3)
+    g = torch.Generator(device="cuda").manual_seed(seed)
     incr = torch.randn(B * L, W, dtype=torch.float64, device="cuda", generator=g) / np.sqrt(L)
     sig, log = (torch.empty(B, dim, dtype=torch.float64, device="cuda") for _ in range(2))
     lie = torch.empty(B, ts, dtype=torch.float64, device="cuda")
@@ -358,9 +358,12 @@ def workload_logsig(pkg, torch, args, peak):
     full = lambda t: pkg.make_tensor_batch(t, dim, 0, D)  # noqa: E731
     lieb = pkg.make_lie_batch(lie, ts, 1, D)
 
+    err, schedule, _ = pkg.signature_tune(st, None, incr, basis, B, length=L, out=sig)
+    err.raise_if_failed()
+
     def run():
-        pkg.signature(st, None, incr, basis, B, length=L, out=sig)
-        pkg.tensor_log_to_lie(st, None, lieb, full(sig), lbasis, basis, B, t2l)
+        pkg.signature(st, None, incr, basis, B, length=L, out=sig).raise_if_failed()
+        pkg.tensor_log_to_lie(st, None, lieb, full(sig), lbasis, basis, B, t2l).raise_if_failed()
 
     stream = torch.cuda.current_stream()
     ms = 1e3 * _time_launches(torch, run, args.steps, args.warmup, stream)
@@ -374,8 +377,9 @@ def workload_logsig(pkg, torch, args, peak):
                                   args.steps, args.warmup, stream)
     ms_t2l = 1e3 * _time_launches(torch, lambda: pkg.tensor_to_lie(st, None, lieb, full(log), lbasis, basis, B, t2l),
                                   args.steps, args.warmup, stream)
-    _line("log-signature paths/sec (W5 D5 L256 FP64): signature + fused ft_log/tensor_to_lie", B / (ms / 1e3),
-          "paths/s", ms, "f64", {"workload": "logsig_w5_d5_l256_b4096"},
+    _line(f"log-signature paths/sec (W{W} D{D} L{L} FP64): signature + fused ft_log/tensor_to_lie", B / (ms / 1e3),
+          "paths/s", ms, "f64", {"workload": f"logsig_w{W}_d{D}_l{L}_b{B}", "schedule": schedule,
+                                 "lie_dim": ts - 1, "t2l_nnz": t2l.nnz()},
           flops=flops, peak=peak,
           extra={"signature_only_ms": ms_sig, "log_to_lie_fused_ms": ms_fused,
                  "log_to_lie_fused_roofline_frac": 2.0 * B * (log_fma + t2l.nnz()) / (ms_fused / 1e3) / 1e12 / peak
@@ -759,13 +763,16 @@ def run_workloads(args):
     peak = _fp64_peak(pkg, 0)
     todo = args.workload.split(",")
     if "all" in todo:
-        todo = ["ft_mul", "logsig", "lie_exp", "ragged", "w6d6", "w2d12", "w16d3", "mixed", "fp32", "adjoints",
-                "shuffle"]
+        todo = ["ft_mul", "logsig", "lie_exp", "ragged", "w6d6", "w2d12", "w16d3", "mixed", "logsig_mixed", "fp32",
+                "adjoints", "shuffle"]
     for w in todo:
         if w == "ft_mul":
             workload_ft_mul(pkg, torch, args, peak)
         elif w == "logsig":
             workload_logsig(pkg, torch, args, peak)
+        elif w == "logsig_mixed":  # the large mixed shapes' log-signatures
+            workload_logsig(pkg, torch, args, peak, 2, 12, 16384, 64, seed=12)
+            workload_logsig(pkg, torch, args, peak, 16, 3, 16384, 64, seed=16)
         elif w == "ragged":
             workload_ragged(pkg, torch, args, peak)
         elif w == "w6d6":

@@ -423,7 +423,8 @@ int rpp_gb_signature_static_scratch(const rpp_gb_plan* plan, rpp_gb_stream strea
  * *threads and *ms (may be NULL) receive the choice and its time per call:
  * threads per CTA in bits 0-9 of *threads, the cap on CTAs per SM (0 = none)
  * in bits 10-13, bit 14 set for the two-launch form, bit 15 set when its
- * forward launch keeps the top level in the output row in global memory, and
+ * forward launch (or a forward-only call) keeps the top level in the output
+ * row in global memory, and
  * for the two-launch form the reverse launch's own CTA size in bits 16-25
  * (0: the same as the forward launch's), and bit 26 set when the launch with
  * the reverse pass keeps the cotangent arrays in a global workspace (the

@@ -168,9 +168,10 @@ struct PathBatch {
 // 0-9 (0: heuristic), a cap on CTAs per SM in bits 10-13 (0: none), and
 // kScheduleSplit: run a forward+reverse call with signature output as a
 // forward launch plus a reverse launch from the final signatures;
-// kScheduleForwardTopGlobal (with kScheduleSplit): the forward launch keeps
-// the top level in the output row in global memory (less shared memory per
-// CTA, more CTAs per SM); with kScheduleSplit, bits 16-25 (when not 0) give
+// kScheduleForwardTopGlobal (with kScheduleSplit, or on a forward-only call):
+// the forward launch keeps the top level in the output row in global memory
+// (less shared memory per CTA, more CTAs per SM); with kScheduleSplit, bits
+// 16-25 (when not 0) give
 // the reverse launch its own CTA size (bits 0-9 then size the forward launch).
 constexpr int kScheduleSplit = 1 << 14;
 constexpr int kScheduleForwardTopGlobal = 1 << 15;

@@ -316,6 +316,11 @@ SigLaunches plan_launches(bool forward, bool has_sig, bool has_seed, bool has_gr
     } else {
         mode |= kBackward | kLoadFinal;
     }
+    // a forward-only call with kScheduleForwardTopGlobal keeps the top level
+    // in the output row (the two-launch form's forward launch does the same)
+    if (threads > 0 && (threads & kScheduleForwardTopGlobal) && mode == (kForward | kTopLevel) &&
+        ((threads >> kScheduleClusterShift) & 7) == 0)
+        mode |= kTopGlobal;
     l.count = 1;
     l.mode[0] = mode;
     const bool letter_kernel = threads == 0 && ((letters && mode == (kForward | kTopLevel)) ||

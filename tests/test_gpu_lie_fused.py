@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 
 pkg = importlib.import_module("rough-path-primitives_gb300")
 
-SHAPES = [(5, 5, 16), (2, 6, 8), (16, 3, 8), (4, 4, 32), (6, 6, 2)]
+SHAPES = [(5, 5, 16), (2, 6, 8), (16, 3, 8), (4, 4, 32), (6, 6, 2), (2, 12, 3)]
 
 
 def _setup(W, D):

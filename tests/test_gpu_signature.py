@@ -590,3 +590,29 @@ def test_fp32_reverse_one_warp_per_letter_agrees_with_shared_memory_kernel(W, D)
     assert np.array_equal(out[0][0], out[1][0]), "signatures differ"
     e = scaled_err(out[0][1], out[1][1])
     assert e <= 2e-6, f"W{W} D{D}: gradients differ by {e:.3e} (scaled)"
+
+
+@pytest.mark.parametrize("W,D,threads", [(2, 12, 512), (5, 5, 128), (4, 4, 256), (16, 3, 128)])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_forward_only_top_level_in_output_row(orc, W, D, threads, dtype):
+    """A forward-only call with schedule bit 15 keeps the top level in the
+    output row instead of shared memory (as the two-launch form's forward
+    launch does): the same arithmetic, so the signatures equal those of the
+    shared-memory form bit for bit, and the oracle's within tolerance; ragged,
+    with empty and unit paths."""
+    rng = np.random.default_rng(W * 71 + D)
+    lengths = np.array([0, 1, 5, 17, 2, 9, 0, 12])
+    offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    incr = rng.normal(0, 0.3, (int(offsets[-1]), W))
+    basis = pkg.TensorBasis(W, D)
+    st = pkg.GB300Strategy(dtype)
+    out = []
+    for schedule in (threads, threads | (1 << 15)):
+        sig = torch.full((len(lengths), basis.size()), float("nan"), dtype=dtype, device="cuda")
+        err = pkg.signature(st, None, dev(incr, dtype), basis, len(lengths), offsets=dev(offsets, torch.int64),
+                            out=sig, schedule=schedule)
+        assert err, err.message
+        out.append(host(sig))
+    assert np.array_equal(out[0], out[1])
+    esig, _ = orc.signature(W, D, incr, offsets)
+    assert_close(out[1], esig, TOL_F64 if dtype == torch.float64 else TOL_F32, f"W{W} D{D} top level in the row")
