@@ -1,6 +1,7 @@
-// signature_letters.cuh -- the FP32 forward step with one warp per first
-// letter (k_signature_letters in signature_fp32.cu, and FP32 forward-only
-// jobs of the grouped launch in signature_group.cu).
+// signature_letters.cuh -- FP32 signatures with one warp per first letter:
+// the forward step (k_signature_letters in signature_fp32.cu, and FP32
+// forward-only jobs of the grouped launch in signature_group.cu) and, below
+// the forward part, the reverse step (k_signature_letters_rev).
 //
 // The same Chen step as signature_body.cuh (Horner chains
 // T^n_j = S_j + T^n_{j-1} (x) x / (n-j+1), S_n <- T^n_n), organised for FP32,
@@ -24,7 +25,10 @@
 //    serves W FMAs with the increment in registers.  No chain reads the top
 //    level, so no other thread needs it.  Level D-1 lives in registers too:
 //    lane l holds its coefficients l, l + 32, ..., which are exactly the
-//    prefixes of its top rows and are read by no other lane.
+//    prefixes of its top rows and are read by no other lane.  Where level
+//    D-2 has 24..32 coefficients per warp (W5 D5, W3 D6) the family form
+//    gives lane u level D-2 coefficient u, its W children and their W^2 top
+//    coefficients instead.
 //  * The increment's W letters are double-buffered by step parity in shared
 //    memory; x_a / m is formed in a register as x_a * (1/m), the single
 //    rounding the shared-memory kernel's scaled increments get.  Each lane
