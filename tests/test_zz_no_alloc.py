@@ -30,7 +30,7 @@ pytestmark = pytest.mark.gpu
 
 pkg = importlib.import_module("rough-path-primitives_gb300")
 
-F64 = 1
+F32, F64 = 0, 1
 
 # CUmemPool_attribute values (cuda.h)
 _POOL_USED_MEM_CURRENT = 7
@@ -73,7 +73,8 @@ def _ragged(rng, B, max_len, W):
 def _call(name, plan, incr, offsets, B, sig, seed, grad, dim, length=0):
     lib = pkg.library()
     stream = torch.cuda.current_stream().cuda_stream
-    rc = getattr(lib, name)(plan, stream, F64, incr.data_ptr(), None if offsets is None else offsets.data_ptr(),
+    dtype = F64 if incr.dtype == torch.float64 else F32
+    rc = getattr(lib, name)(plan, stream, dtype, incr.data_ptr(), None if offsets is None else offsets.data_ptr(),
                             length, B, sig.data_ptr(), dim, seed.data_ptr(), dim, grad.data_ptr())
     msg = lib.rpp_gb_last_error_string()
     return rc, (msg.decode() if msg else "")
@@ -175,6 +176,34 @@ def test_static_scratch_after_tuning(W, D, B, max_len):
         rc, msg = _static_call_without_pool_growth(pool, plan, incr, offsets, B, sig, seed, grad, dim)
         assert rc == 0, f"schedule {chosen.value:#x}, call {call}: {msg}"
         _assert_same(sig, grad, sig_ref, grad_ref, f"schedule {chosen.value:#x}, call {call}")
+
+
+@pytest.mark.parametrize("W,D", [(5, 5), (8, 4)])
+def test_static_scratch_fp32_warp_per_letter_kernel(W, D):
+    """FP32 calls of these shapes take the warp-per-letter forward + reverse
+    kernel without a recorded schedule; through the allocation-free entry
+    point they run the same kernel (results equal bit for bit) and allocate
+    nothing."""
+    B = 200
+    rng = np.random.default_rng(W * 31 + D)
+    offsets_h, incr_h = _ragged(rng, B, 40, W)
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    plan = basis.plan(0)
+    incr = torch.from_numpy(incr_h).to("cuda", torch.float32)
+    offsets = torch.from_numpy(offsets_h).cuda()
+    seed = torch.from_numpy(rng.uniform(-1, 1, (B, dim))).to("cuda", torch.float32)
+    sig_ref = torch.full((B, dim), float("nan"), dtype=torch.float32, device="cuda")
+    grad_ref = torch.full_like(incr, float("nan"))
+    rc, msg = _call("rpp_gb_signature", plan, incr, offsets, B, sig_ref, seed, grad_ref, dim)
+    assert rc == 0, msg
+    pool = _PoolWatch()
+    sig = torch.full_like(sig_ref, float("nan"))
+    grad = torch.full_like(grad_ref, float("nan"))
+    rc, msg = _static_call_without_pool_growth(pool, plan, incr, offsets, B, sig, seed, grad, dim)
+    assert rc == 0, msg
+    torch.cuda.synchronize()
+    assert torch.equal(sig, sig_ref) and torch.equal(grad, grad_ref)
 
 
 def test_static_scratch_refuses_what_needs_an_allocation():
