@@ -350,3 +350,54 @@ def test_products_large_batches(orc, dtype, tol, W, D, n):
     e = np.zeros((n, stride))
     orc.ft_fma(W, D, e, z, x, y, (full, full, full, full), 0.25, 0.75)
     assert_close(host(out)[:, :dim], e[:, :dim], tol, f"ft_fma W{W}D{D} n{n}")
+
+
+def test_dependent_products_in_a_graph(orc):
+    """A chain in which every product reads the one before it -- with an
+    in-place product and a non-product kernel in between -- gives the oracle's
+    chain, eagerly and from a CUDA graph, and the two agree bit for bit."""
+    W, D, n = 4, 4, 1024
+    basis = pkg.TensorBasis(W, D)
+    dim = basis.size()
+    full = (0, D)
+    rng = np.random.default_rng(404)
+    a_h, b_h = (rng.uniform(-0.5, 0.5, (n, dim)) for _ in range(2))
+    st = pkg.GB300Strategy(torch.float64)
+    a, b = dev(a_h, torch.float64), dev(b_h, torch.float64)
+    x1, x2, x4 = (torch.zeros(n, dim, dtype=torch.float64, device="cuda") for _ in range(3))
+
+    def chain(cfg):
+        t = lambda v: tb(v, dim, full)  # noqa: E731
+        pkg.ft_mul(st, cfg, t(x1), t(a), t(b), basis, n).raise_if_failed()
+        pkg.ft_mul(st, cfg, t(x2), t(x1), t(b), basis, n).raise_if_failed()
+        pkg.ft_inplace_mul(st, cfg, t(x2), t(a), basis, n).raise_if_failed()
+        x2.mul_(0.5)
+        pkg.ft_fma(st, cfg, t(x4), t(x2), t(x1), t(x2), basis, n).raise_if_failed()
+
+    chain(None)
+    eager = host(x4).copy()
+    # the oracle's chain
+    e1, e2, e4 = (np.zeros((n, dim)) for _ in range(3))
+    rr = (full, full, full)
+    orc.ft_mul(W, D, e1, a_h, b_h, rr)
+    orc.ft_mul(W, D, e2, e1, b_h, rr)
+    e3 = np.zeros((n, dim))
+    orc.ft_mul(W, D, e3, e2, a_h, rr)
+    e3 *= 0.5
+    orc.ft_fma(W, D, e4, e3, e1, e3, (full, full, full, full))
+    assert_close(eager, e4, TOL_F64, "dependent chain, eager")
+    # the same chain captured in a graph and replayed
+    for v in (x1, x2, x4):
+        v.zero_()
+    cap = torch.cuda.Stream()
+    cap.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(cap):
+        cfg = pkg.DeviceLaunchConfig(cap)
+        with torch.cuda.graph(graph, stream=cap):
+            chain(cfg)
+    torch.cuda.current_stream().wait_stream(cap)
+    for v in (x1, x2, x4):
+        v.fill_(float("nan"))
+    graph.replay()
+    assert np.array_equal(host(x4), eager)
