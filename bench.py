@@ -573,7 +573,9 @@ def workload_mixed(pkg, torch, args, peak):
     sep = _graph_of(torch, separate)
     ms_sep = 1e3 * _time_launches(torch, sep.replay, args.steps, args.warmup, cur)
     cands = []
-    for t_deep in (256, 384, 512):
+    # the deep job's team size, with its cotangent arrays in shared memory or
+    # (bit 26) in a global workspace, as its tuned separate call may have them
+    for t_deep in (256, 384, 512, 256 | (1 << 26), 320 | (1 << 26), 512 | (1 << 26)):
         jobs = [pkg.SignatureJob(st, incr, basis, B, length=L, out=sig, seed=ell, grad=grad,
                                  threads=t_deep if basis.width == 2 else 128)
                 for basis, incr, ell, sig, grad, _ in parts]

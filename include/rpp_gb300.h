@@ -459,21 +459,24 @@ int rpp_gb_signature_with_schedule(const rpp_gb_plan* plan, rpp_gb_stream stream
  * plan (width, depth), dtype, equal-length or ragged increments, outputs --
  * so one launch covers batches of different (width, depth) and of FP64 and
  * FP32 together, e.g. inside one captured CUDA graph.  Each path of job j is
- * run by a team of `threads` threads (a multiple of 32, at least
+ * run by a team of `threads` threads (bits 0-9: a multiple of 32, at least
  * width*depth; 0: the CTA size of the schedule recorded for that shape by
- * rpp_gb_signature_tune, else a heuristic); a CTA holds as many teams of the
+ * rpp_gb_signature_tune, else a heuristic; bit 26, or a recorded one-launch
+ * schedule with bit 26, on an FP64 forward + reverse job: its cotangent level
+ * and chains in a stream-ordered global workspace, one slice per team, so
+ * more teams of a deep state fit per SM); a CTA holds as many teams of the
  * job in progress as its threads and shared memory allow, so small states
  * keep many paths per SM beside large ones.  CTAs take the jobs in order of
  * their most expensive path and, inside a job, paths longest first from a
  * work counter.  Each job's outputs equal, bit for bit, those of a separate
  * rpp_gb_signature call with `threads` threads per CTA (and the same
- * reverse-step form).  `schedule`: threads per CTA in bits 0-9 (at most 640;
+ * reverse-step form and cotangent placement).  `schedule`: threads per CTA in bits 0-9 (at most 640;
  * 0: 640) and bit 27 for the D-barrier reverse step.  Limits: 1 to 8 jobs,
  * all plans on one device, each job's state in one team's shared memory
  * (RPP_GB_NOT_IMPLEMENTED otherwise, e.g. width 6 depth 6 in FP64: run it
  * with rpp_gb_signature), fewer than 2^31 paths per job.  Stream-ordered;
- * the job order and work counters are allocated stream-ordered and released
- * after the launch. */
+ * the job order, work counters and cotangent workspaces are allocated
+ * stream-ordered and released after the launch. */
 typedef struct rpp_gb_signature_job {
     const rpp_gb_plan* plan;
     int32_t dtype;

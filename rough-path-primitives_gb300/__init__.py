@@ -669,7 +669,9 @@ class SignatureJob:
     """One job of ``signature_group``: the arguments of one ``signature`` call
     (its strategy -- hence dtype --, basis, increments with ``length`` or
     ``offsets``, outputs) and ``threads``, the threads that run one of its
-    paths (0: the shape's tuned CTA size, else a heuristic)."""
+    paths (0: the shape's tuned CTA size, else a heuristic), with bit 26 for
+    an FP64 forward + reverse job whose cotangent arrays go to a global
+    workspace."""
 
     def __init__(self, strategy, increments, basis, num_batches, *, length=None, offsets=None, out=None,
                  out_stride=None, seed=None, seed_stride=None, grad=None, threads=0):

@@ -1388,7 +1388,13 @@ int rpp_gb_signature_group(rpp_gb_stream stream, const rpp_gb_signature_job* job
                                                          job.sig_stride, job.seed, job.seed_stride, job.grad, true);
         if (rc) return fail(rc, which + rpp_gb_last_error_string());
         const auto& g = job.plan->geometry;
-        int t = job.threads;
+        // threads per team in bits 0-9; bit 26 (kScheduleCotangentGlobal):
+        // an FP64 forward + reverse job keeps its cotangent arrays in a global
+        // workspace (as the schedule bit of rpp_gb_signature does)
+        int t = job.threads & 1023;
+        bool cot = (job.threads & rpp_gb::kScheduleCotangentGlobal) != 0;
+        if (job.threads < 0 || (job.threads & ~(1023 | rpp_gb::kScheduleCotangentGlobal)) != 0)
+            return fail(RPP_GB_INVALID_ARGUMENT, which + "threads: a team size in bits 0-9, optionally bit 26");
         // FP32 forward-only jobs of an instantiated shape: one warp per first
         // letter (the kernel of rpp_gb_signature's schedule bit 16), unless
         // the caller asks for a team size
@@ -1396,8 +1402,12 @@ int rpp_gb_signature_group(rpp_gb_stream stream, const rpp_gb_signature_job* job
                              rpp_gb::letter_warps_supported(g.width, g.depth) && 32 * g.width <= cta;
         if (letters) t = 32 * g.width;
         if (t == 0) {
-            // the recorded schedule's (forward) CTA size, else the heuristic
-            t = scheduled_threads(schedule_key(job.plan, job.dtype, true, job.sig, job.seed, job.offsets)) & 1023;
+            // the recorded schedule's (forward) CTA size and cotangent
+            // workspace, else the heuristic
+            const int rec = scheduled_threads(schedule_key(job.plan, job.dtype, true, job.sig, job.seed, job.offsets));
+            t = rec & 1023;
+            if (!(rec & rpp_gb::kScheduleSplit) && ((rec >> rpp_gb::kScheduleClusterShift) & 7) == 0)
+                cot = cot || (rec & rpp_gb::kScheduleCotangentGlobal) != 0;
             if (t == 0)
                 for (t = 32; t < 256 && static_cast<uint32_t>(t) < g.pw[g.depth];) t *= 2;
             t = std::max(t, (g.depth * g.width + 31) / 32 * 32);
@@ -1409,6 +1419,7 @@ int rpp_gb_signature_group(rpp_gb_stream stream, const rpp_gb_signature_job* job
         in[j] = rpp_gb::SignatureJob{g, job.dtype == RPP_GB_F64, t, letters, job.incr,
                                      rpp_gb::PathBatch{job.offsets, job.length, job.batch}, job.sig, job.sig_stride,
                                      job.seed, job.seed_stride, job.grad};
+        in[j].cot = cot && job.dtype == RPP_GB_F64 && job.seed && job.grad;
     }
     DeviceGuard guard(device);
     if (guard.error() != cudaSuccess) return cuda_status(guard.error(), "cudaSetDevice");

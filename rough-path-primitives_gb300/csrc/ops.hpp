@@ -235,6 +235,10 @@ struct SignatureJob {
     const void* seed;
     int64_t seed_stride;
     void* grad;
+    // FP64 forward + reverse: the cotangent level and chains in a per-team
+    // slice of a global workspace (kScheduleCotangentGlobal), the state and
+    // forward chains in the team's shared memory
+    bool cot = false;
 };
 // Refusal reasons beside the CUDA status.
 enum class GroupRefusal : int { None = 0, StateTooLarge = 1, TooManyPaths = 2 };

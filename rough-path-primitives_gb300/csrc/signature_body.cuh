@@ -972,7 +972,7 @@ __device__ __forceinline__ void backward_step_merged(const Team& tm, const SigGe
 // Fills 1/m and m; ends with a barrier.
 template <typename T, int WT, bool COT, typename Team>
 __device__ __forceinline__ SigShared<T> place_arrays(const Team& tm, const SigGeometry& sg, int mode, T* gws, int64_t gws_stride,
-                                                     unsigned char* smem_raw, bool& vec4) {
+                                                     unsigned char* smem_raw, bool& vec4, int64_t slot = -1) {
     const Geometry& G = sg.g;
     const int D = G.depth;
     const uint32_t W = static_cast<uint32_t>(G.width);
@@ -984,7 +984,9 @@ __device__ __forceinline__ SigShared<T> place_arrays(const Team& tm, const SigGe
     // kCotGlobal: S and the forward chains in shared memory, the cotangent
     // level and chains in this CTA's slice of the global workspace
     const bool cot_global = COT && (mode & kCotGlobal) && bwd && gws;
-    T* p = (gws && !cot_global) ? gws + blockIdx.x * gws_stride : q;
+    // the workspace slice: the CTA's, or `slot`'s (a team of the grouped launch)
+    const int64_t ws_slot = slot >= 0 ? slot : static_cast<int64_t>(blockIdx.x);
+    T* p = (gws && !cot_global) ? gws + ws_slot * gws_stride : q;
     // the FP32 four-coefficient forward step wants S + 1, Tf + choff[1] and the
     // scaled increments on 16-byte boundaries (kVec4; the host adds slack)
     vec4 = false;
@@ -1001,7 +1003,7 @@ __device__ __forceinline__ SigShared<T> place_arrays(const Team& tm, const SigGe
     sh.Tf = p;
     p += sg.chain_total;
     if (bwd) {
-        T* g = cot_global ? gws + blockIdx.x * gws_stride : p;
+        T* g = cot_global ? gws + ws_slot * gws_stride : p;
         sh.G = g;
         g += lo;
         sh.Tb = g;

@@ -28,6 +28,7 @@ struct GroupJob {
     int32_t fp64;
     int32_t mode;
     int32_t letters;      // FP32 forward-only: warp-per-letter teams (signature_letters.cuh)
+    int32_t cot;          // FP64 forward + reverse: cotangent arrays in the workspace gws
     uint32_t team_threads;
     uint32_t teams;
     uint32_t slice;       // shared-memory bytes of one team (a multiple of 16)
@@ -45,6 +46,8 @@ struct GroupJob {
     void* grad;
     int32_t* order;         // ragged jobs: the paths longest first (scratch)
     unsigned int* counter;  // the job's work counter (scratch)
+    void* gws;              // cot jobs: one slice of gws_stride elements per team of the launch
+    int64_t gws_stride;
 };
 
 struct GroupTable {
@@ -162,12 +165,15 @@ constexpr int kGroupMaxTeams = 15;  // named barriers 1..15
 // Team k's share of the current job: paths from the job's counter until none
 // is left.  Not inlined: each (precision, width) body gets its own register
 // allocation (inlined into one kernel, the sixteen bodies spilled).
-template <typename T, int WT>
+// COT: the job keeps its cotangent level and chains in team slot
+// blockIdx.x * teams + k of the workspace (kCotGlobal).
+template <typename T, int WT, bool COT = false>
 __device__ __noinline__ void group_team(const SubTeam tm, const uint32_t k) {
     const GroupJob& job = g_job;
     bool vec4 = false;
-    SigShared<T> sh = place_arrays<T, WT, false>(tm, g_sg, job.mode, static_cast<T*>(nullptr), 0,
-                                                 g_group_smem + static_cast<size_t>(k) * job.slice, vec4);
+    SigShared<T> sh = place_arrays<T, WT, COT>(tm, g_sg, job.mode, COT ? static_cast<T*>(job.gws) : nullptr,
+                                               job.gws_stride, g_group_smem + static_cast<size_t>(k) * job.slice,
+                                               vec4, static_cast<int64_t>(blockIdx.x) * job.teams + k);
     for (;;) {
         if (tm.rank() == 0) g_task[k] = static_cast<int64_t>(atomicAdd(job.counter, 1u));
         tm.sync();
@@ -225,6 +231,21 @@ __device__ __forceinline__ void group_team_width(const SubTeam tm, const uint32_
             return;
         }
     }
+    if constexpr (std::is_same<T, double>::value) {
+        if (g_job.cot) {
+            switch (g_job.width) {
+                case 2: group_team<T, 2, true>(tm, k); break;
+                case 3: group_team<T, 3, true>(tm, k); break;
+                case 4: group_team<T, 4, true>(tm, k); break;
+                case 5: group_team<T, 5, true>(tm, k); break;
+                case 6: group_team<T, 6, true>(tm, k); break;
+                case 8: group_team<T, 8, true>(tm, k); break;
+                case 16: group_team<T, 16, true>(tm, k); break;
+                default: group_team<T, 0, true>(tm, k); break;
+            }
+            return;
+        }
+    }
     switch (g_job.width) {
         case 2: group_team<T, 2>(tm, k); break;
         case 3: group_team<T, 3>(tm, k); break;
@@ -271,11 +292,12 @@ size_t letter_slice_bytes(int width, int depth) {
 
 // One team's shared memory for `job` (mode may gain kTopGlobal when the top
 // level must go to global memory to fit `budget`); 0 when it cannot fit.
+// With kCotGlobal the cotangent arrays are not in shared memory.
 template <typename T>
 size_t group_slice(const SigGeometry& sg, int threads, int& mode, size_t budget) {
-    const bool bwd = mode & kBackward;
-    size_t smem = sig_smem_bytes<T>(sg, threads, bwd, true, false);
-    if (smem > budget) {
+    const bool bwd = (mode & kBackward) && !(mode & kCotGlobal);
+    size_t smem = sig_smem_bytes<T>(sg, threads, bwd, true, (mode & kTopGlobal) != 0);
+    if (smem > budget && !(mode & kTopGlobal)) {
         mode |= kTopGlobal;
         smem = sig_smem_bytes<T>(sg, threads, bwd, true, true);
     }
@@ -308,8 +330,21 @@ cudaError_t launch_signature_group(const DeviceInfo& dev, cudaStream_t s, const 
         const SigGeometry sg = make_sig_geometry(in.g);
         job.mode = kForward | (in.sig ? kTopLevel : 0) | (in.seed && in.grad ? kBackward : 0);
         if ((schedule & kScheduleMergedReverse) && (job.mode & kBackward)) job.mode |= kMergedReverse;
+        job.cot = in.cot && in.fp64 && (job.mode & kBackward) && !in.letters ? 1 : 0;
+        if (job.cot) job.mode |= kCotGlobal;
         int mode = job.mode;
         size_t slice = in.fp64 ? group_slice<double>(sg, t, mode, optin) : group_slice<float>(sg, t, mode, optin);
+        if (job.cot && slice && !(mode & kTopGlobal)) {
+            // the top level in the signature and seed rows where that lets
+            // more teams share a CTA (W2 D12: 131 -> 98 KB, two teams of 256)
+            int m2 = mode | kTopGlobal;
+            const size_t s2 = group_slice<double>(sg, t, m2, optin);
+            const size_t fit = static_cast<size_t>(cta / t);
+            if (s2 && std::min(fit, optin / s2) > std::min(fit, optin / slice)) {
+                mode = m2;
+                slice = s2;
+            }
+        }
         if (in.letters) {
             if (in.fp64 || job.mode != (kForward | kTopLevel) || t != 32 * in.g.width)
                 return cudaErrorInvalidConfiguration;
@@ -367,19 +402,35 @@ cudaError_t launch_signature_group(const DeviceInfo& dev, cudaStream_t s, const 
         return err;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int64_t ctas = std::min<int64_t>(needed_ctas, static_cast<int64_t>(per_sm) * dev.sm_count);
-    // scratch: the counters and the job sequence, then the ragged orders
+    // scratch: the counters and the job sequence, the ragged orders, then the
+    // cot jobs' workspaces (one slice per team of the launch; at W2 D12 FP64,
+    // 98 KB a slice, 30 MB for two teams on each of 152 SMs: L2-resident)
+    size_t ws_bytes = 0;
+    const size_t orders_bytes = (static_cast<size_t>(ragged) * sizeof(int32_t) + 255) / 256 * 256;
+    for (int j = 0; j < njobs; ++j) {
+        GroupJob& job = tab.job[j];
+        if (!job.cot) continue;
+        const SigGeometry sg = make_sig_geometry(jobs[j].g);
+        job.gws_stride = static_cast<int64_t>((sg.g.db[sg.g.depth] + sg.chain_total + 31) / 32 * 32);
+        ws_bytes += static_cast<size_t>(ctas) * job.teams * job.gws_stride * sizeof(double);
+    }
     void* scratch = nullptr;
-    err = cudaMallocAsync(&scratch, 256 + static_cast<size_t>(ragged) * sizeof(int32_t), s);
+    err = cudaMallocAsync(&scratch, 256 + orders_bytes + ws_bytes, s);
     if (err != cudaSuccess) return err;
     char* base = static_cast<char*>(scratch);
     tab.seq = reinterpret_cast<int32_t*>(base + 128);
     int32_t* order = reinterpret_cast<int32_t*>(base + 256);
+    char* ws = base + 256 + orders_bytes;
     for (int j = 0; j < njobs; ++j) {
         GroupJob& job = tab.job[j];
         job.counter = reinterpret_cast<unsigned int*>(base) + j;
         if (job.offsets && job.batch > 0) {
             job.order = order;
             order += job.batch;
+        }
+        if (job.cot) {
+            job.gws = ws;
+            ws += static_cast<size_t>(ctas) * job.teams * job.gws_stride * sizeof(double);
         }
     }
     k_order_group<<<1, 1024, 0, s>>>(tab);

@@ -95,6 +95,21 @@ def test_mixed_shapes_forward_and_reverse(orc):
     run_group_and_separate(orc, jobs)
 
 
+def test_cotangent_workspace_jobs(orc):
+    """FP64 forward + reverse jobs with bit 26 on their threads keep the
+    cotangent level and chains in a per-team slice of a global workspace (the
+    form the tuner picks for width 2 depth 12 as a separate call): outputs
+    equal a separate call with that schedule bit for bit, beside a job in
+    shared memory; ragged, with empty paths."""
+    rng = np.random.default_rng(58)
+    cot = 1 << 26
+    jobs = [make_job(rng, 2, 12, 24, torch.float64, L=16, threads=256 | cot),
+            make_job(rng, 16, 3, 40, torch.float64, L=16, threads=128),
+            make_job(rng, 3, 4, 50, torch.float64, ragged=(0, 30), threads=128 | cot)]
+    run_group_and_separate(orc, jobs)
+    run_group_and_separate(orc, jobs, schedule=640 | (1 << 27))
+
+
 def test_fp64_and_fp32_ragged_forward(orc):
     """The uneven-length workload at test size: width 8 depth 4, lengths
     U{1..150}, one FP64 and one FP32 batch in one launch."""
@@ -191,6 +206,9 @@ def test_group_refusals():
     assert not err and err.code == pkg.ErrorCode.InvalidArgument
     odd = make_job(rng, 2, 3, 2, torch.float64, L=4, threads=48)
     err = pkg.signature_group(None, [as_job(odd, device_args(odd))])
+    assert not err and err.code == pkg.ErrorCode.InvalidArgument
+    flagged = make_job(rng, 2, 3, 2, torch.float64, L=4, threads=64 | (1 << 20))  # not a job bit
+    err = pkg.signature_group(None, [as_job(flagged, device_args(flagged))])
     assert not err and err.code == pkg.ErrorCode.InvalidArgument
     err = pkg.signature_group(None, [as_job(small, a)], schedule=768)
     assert not err and err.code == pkg.ErrorCode.InvalidArgument
