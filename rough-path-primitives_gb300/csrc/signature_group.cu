@@ -334,11 +334,13 @@ cudaError_t launch_signature_group(const DeviceInfo& dev, cudaStream_t s, const 
         if (job.cot) job.mode |= kCotGlobal;
         int mode = job.mode;
         size_t slice = in.fp64 ? group_slice<double>(sg, t, mode, optin) : group_slice<float>(sg, t, mode, optin);
-        if (job.cot && slice && !(mode & kTopGlobal)) {
+        if (slice && !in.letters && !(mode & kTopGlobal)) {
             // the top level in the signature and seed rows where that lets
-            // more teams share a CTA (W2 D12: 131 -> 98 KB, two teams of 256)
+            // more teams share a CTA (W2 D12 with its cotangents in the
+            // workspace: 131 -> 98 KB, two teams of 256; W8 D4 FP64 forward:
+            // 75 -> 42 KB, five teams of 128 instead of three)
             int m2 = mode | kTopGlobal;
-            const size_t s2 = group_slice<double>(sg, t, m2, optin);
+            const size_t s2 = in.fp64 ? group_slice<double>(sg, t, m2, optin) : group_slice<float>(sg, t, m2, optin);
             const size_t fit = static_cast<size_t>(cta / t);
             if (s2 && std::min(fit, optin / s2) > std::min(fit, optin / slice)) {
                 mode = m2;
