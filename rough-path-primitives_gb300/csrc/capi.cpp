@@ -363,7 +363,7 @@ int tune_signature(const rpp_gb_plan* plan, cudaStream_t s, int32_t dtype, const
     // a reverse pass with the cotangent arrays in a global workspace (fused
     // form, and the two-launch form's reverse launch)
     if (seed && grad)
-        for (int t : {256, 512}) {
+        for (int t : {256, 320, 384, 512}) {
             candidates[ncand++] = t | rpp_gb::kScheduleCotangentGlobal;
             if (sig)  // the two-launch form: this forward size with a 512-thread reverse launch too
                 for (int rev : {0, 512})
