@@ -503,10 +503,13 @@ __device__ __forceinline__ void letter_path(const float* __restrict__ incr, int6
 // first letter, so warp c runs the step on its slice alone; only the letter
 // gradient sums over all slices (a butterfly in the warp, then W warps'
 // partials added in warp order once per 8 steps, after one CTA barrier).
-// The kernel is bound by shared-memory instructions, so everything a lane
-// alone reads lives in its registers: the seed's top rows (constant through
-// the pass), and of S and G level D-1 (lane l: rows l, l + 32, ...) and the
-// lane's own coefficients of levels 1..D-2 (l, l + 32, ... of each level).
+// Shared-memory instructions bounded the first form of this kernel (with the
+// lower levels of S and G and a table of x_a / m in shared memory), so
+// everything a lane alone reads lives in its registers: the seed's top rows
+// (constant through the pass), and of S and G level D-1 (lane l: rows l,
+// l + 32, ...) and the lane's own coefficients of levels 1..D-2 (l, l + 32,
+// ... of each level); the family form (LetterRevLayout::family) regroups
+// levels D-2..D by families.
 // Scaled increments x_a / m are formed in registers (x_a * (1/m), rounded
 // once).  Shared memory holds only what other lanes read: the increment, the
 // chains T^n_j of levels 1..D-2 and the cotangent chains A^n_j of levels
