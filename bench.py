@@ -39,10 +39,13 @@ WIDTH, DEPTH, BATCH, LENGTH = 5, 5, 4096, 256
 # DRAM bytes of one headline step under the two-launch schedule, from a
 # one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, nine steps)
 # of `python bench.py --steps 2 --warmup 3 --no-cpu-baseline --no-plain
-# --schedule 16512`: forward launch 42.8 MB read + 65.5 MB written, reverse
-# launch 199.0 MB read + 28.0 MB written: the compulsory inputs and outputs,
-# with the seed's top level re-read from L2, not DRAM.
-TWO_LAUNCH_TRAFFIC_BYTES = 335.3e6
+# --schedule 134267008` (the tuner's schedule: two launches, 128 threads, the
+# forward launch's top level in the output row, the D-barrier reverse step):
+# forward launch 44.3 MB read + 83.1 MB written, reverse launch 199.7 MB read +
+# 30.9 MB written -- the compulsory inputs and outputs, the seed's top level
+# re-read from L2, not DRAM.  (Schedule 16512, without the top level in the
+# row: 335.3 MB.)
+TWO_LAUNCH_TRAFFIC_BYTES = 358.0e6
 METRIC = "signature fwd+bwd paths/sec (d=5,N=5,L=256) fused vs plain; % of roofline"
 
 
@@ -1068,7 +1071,7 @@ def main():
         "roofline": {"bound": "fp64_fma", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": (achieved / fp64_peak) if fp64_peak else None,
                      "traffic": TWO_LAUNCH_TRAFFIC_BYTES if tuned_threads & (1 << 14) else None,
-                     "traffic_unit": "DRAM bytes per step (both launches), ncu capture of the two-launch schedule",
+                     "traffic_unit": "DRAM bytes per step (both launches), ncu capture of the tuned two-launch schedule",
                      "peak_source": "measured in-run (rpp_gb_fma_peak, FP64 FMA chains)",
                      "algorithmic_flops_per_launch": flops_per_launch,
                      "fma_per_path": fma_per_path},
