@@ -1395,11 +1395,13 @@ int rpp_gb_signature_group(rpp_gb_stream stream, const rpp_gb_signature_job* job
         bool cot = (job.threads & rpp_gb::kScheduleCotangentGlobal) != 0;
         if (job.threads < 0 || (job.threads & ~(1023 | rpp_gb::kScheduleCotangentGlobal)) != 0)
             return fail(RPP_GB_INVALID_ARGUMENT, which + "threads: a team size in bits 0-9, optionally bit 26");
-        // FP32 forward-only jobs of an instantiated shape: one warp per first
-        // letter (the kernel of rpp_gb_signature's schedule bit 16), unless
-        // the caller asks for a team size
-        const bool letters = t == 0 && job.dtype == RPP_GB_F32 && job.sig && !job.seed &&
-                             rpp_gb::letter_warps_supported(g.width, g.depth) && 32 * g.width <= cta;
+        // FP32 jobs of an instantiated shape: one warp per first letter (the
+        // kernels of rpp_gb_signature's schedule bit 16: forward-only, and
+        // forward + reverse for depth >= 3), unless the caller asks for a
+        // team size
+        const bool letters = t == 0 && job.dtype == RPP_GB_F32 && 32 * g.width <= cta &&
+                             ((job.sig && !job.seed && rpp_gb::letter_warps_supported(g.width, g.depth)) ||
+                              (job.seed && rpp_gb::letter_reverse_supported(g.width, g.depth)));
         if (letters) t = 32 * g.width;
         if (t == 0) {
             // the recorded schedule's (forward) CTA size and cotangent

@@ -227,7 +227,8 @@ struct SignatureJob {
     Geometry g;
     bool fp64;
     int threads;  // team size (a multiple of 32, at least width * depth)
-    bool letters;  // FP32 forward-only: a team of width warps, one per first letter (threads = 32 width)
+    bool letters;  // FP32: a team of width warps, one per first letter (threads = 32 width; forward-only, or
+                   // forward + reverse at depth >= 3)
     const void* incr;
     PathBatch paths;
     void* sig;

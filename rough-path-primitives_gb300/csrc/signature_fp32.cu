@@ -75,8 +75,8 @@ __global__ void __launch_bounds__(W * 32, letter_rev_min_blocks(W))
         const int64_t b = paths.order ? paths.order[slot] : slot;
         const int64_t off = paths.offsets ? paths.offsets[b] : b * paths.length;
         const int64_t len = paths.offsets ? paths.offsets[b + 1] - off : paths.length;
-        letter_fwd_bwd<W, D>(incr, b, off, len, sig, sig_stride, seed, seed_stride, grad, mode, region, pbuf, c,
-                             lane);
+        letter_fwd_bwd<W, D>(CtaTeam{}, incr, b, off, len, sig, sig_stride, seed, seed_stride, grad, mode, region,
+                             pbuf, c, lane);
         __syncthreads();  // the last block's partials are read before the next path writes pbuf
         if (paths.counter) {
             if (threadIdx.x == 0) s_next = static_cast<int64_t>(atomicAdd(paths.counter, 1u));

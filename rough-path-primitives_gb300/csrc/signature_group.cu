@@ -27,7 +27,7 @@ struct GroupJob {
     int32_t depth;
     int32_t fp64;
     int32_t mode;
-    int32_t letters;      // FP32 forward-only: warp-per-letter teams (signature_letters.cuh)
+    int32_t letters;      // FP32: warp-per-letter teams (signature_letters.cuh), forward-only or forward + reverse
     int32_t cot;          // FP64 forward + reverse: cotangent arrays in the workspace gws
     uint32_t team_threads;
     uint32_t teams;
@@ -213,7 +213,51 @@ __device__ __noinline__ void group_letters(const SubTeam tm, const uint32_t k) {
     }
 }
 
+// Team k of W warps on FP32 forward + reverse paths of the current job (the
+// kernel k_signature_letters_rev, inside the group): the warps meet on the
+// team's named barrier once per 8 reverse steps (the letter gradients) and
+// to take the next path.
+template <int W, int D>
+__device__ __noinline__ void group_letters_rev(const SubTeam tm, const uint32_t k) {
+    using Rev = LetterRevLayout<W, D>;
+    const GroupJob& job = g_job;
+    const uint32_t c = tm.rank() / 32, lane = tm.rank() % 32;
+    float* base = reinterpret_cast<float*>(g_group_smem + static_cast<size_t>(k) * job.slice);
+    float* region = base + c * Rev::warp_floats;
+    float* pbuf = base + W * Rev::warp_floats;
+    for (;;) {
+        if (tm.rank() == 0) g_task[k] = static_cast<int64_t>(atomicAdd(job.counter, 1u));
+        tm.sync();
+        const int64_t idx = g_task[k];
+        tm.sync();  // every warp has read the slot before the leader rewrites it
+        if (idx >= job.batch) break;
+        const int64_t b = job.order ? job.order[idx] : idx;
+        const int64_t off = job.offsets ? job.offsets[b] : b * job.length;
+        const int64_t len = job.offsets ? job.offsets[b + 1] - off : job.length;
+        letter_fwd_bwd<W, D>(tm, static_cast<const float*>(job.incr), b, off, len, static_cast<float*>(job.sig),
+                             job.sig_stride, static_cast<const float*>(job.seed), job.seed_stride,
+                             static_cast<float*>(job.grad), job.mode & (kForward | kBackward | kTopLevel), region,
+                             pbuf, c, lane);
+        tm.sync();  // the last block's partials are read before the next path writes pbuf
+    }
+}
+
+template <int W, int D>
+__device__ __forceinline__ void group_letters_rev_if(const SubTeam tm, const uint32_t k) {
+    if constexpr (D >= 3) group_letters_rev<W, D>(tm, k);
+}
+
 __device__ __forceinline__ void group_letters_shape(const SubTeam tm, const uint32_t k) {
+    if (g_job.mode & kBackward) {
+        switch (g_job.width * 100 + g_job.depth) {
+#define RPP_GB_LETTER_CASE(w, d) \
+    case w * 100 + d: group_letters_rev_if<w, d>(tm, k); break;
+            RPP_GB_LETTER_SHAPES(RPP_GB_LETTER_CASE)
+#undef RPP_GB_LETTER_CASE
+            default: break;
+        }
+        return;
+    }
     switch (g_job.width * 100 + g_job.depth) {
 #define RPP_GB_LETTER_CASE(w, d) \
     case w * 100 + d: group_letters<w, d>(tm, k); break;
@@ -290,6 +334,28 @@ size_t letter_slice_bytes(int width, int depth) {
     }
 }
 
+// The same for a forward + reverse team (the W warps' regions and the
+// team's letter-partials buffer), 0 without a reverse instantiation.
+template <int W, int D>
+size_t letter_rev_slice_bytes_shape() {
+    if constexpr (D >= 3) {
+        using Rev = LetterRevLayout<W, D>;
+        return ((static_cast<size_t>(W) * Rev::warp_floats + Rev::pbuf_floats) * sizeof(float) + 15) / 16 * 16;
+    } else {
+        return 0;
+    }
+}
+
+size_t letter_rev_slice_bytes(int width, int depth) {
+    switch (width * 100 + depth) {
+#define RPP_GB_LETTER_CASE(w, d) \
+    case w * 100 + d: return letter_rev_slice_bytes_shape<w, d>();
+        RPP_GB_LETTER_SHAPES(RPP_GB_LETTER_CASE)
+#undef RPP_GB_LETTER_CASE
+        default: return 0;
+    }
+}
+
 // One team's shared memory for `job` (mode may gain kTopGlobal when the top
 // level must go to global memory to fit `budget`); 0 when it cannot fit.
 // With kCotGlobal the cotangent arrays are not in shared memory.
@@ -348,9 +414,12 @@ cudaError_t launch_signature_group(const DeviceInfo& dev, cudaStream_t s, const 
             }
         }
         if (in.letters) {
-            if (in.fp64 || job.mode != (kForward | kTopLevel) || t != 32 * in.g.width)
+            // forward-only, or forward + reverse (depth >= 3), in FP32 with
+            // one warp per first letter
+            const bool rev = job.mode & kBackward;
+            if (in.fp64 || !(job.mode & kForward) || (!rev && !(job.mode & kTopLevel)) || t != 32 * in.g.width)
                 return cudaErrorInvalidConfiguration;
-            slice = letter_slice_bytes(in.g.width, in.g.depth);
+            slice = rev ? letter_rev_slice_bytes(in.g.width, in.g.depth) : letter_slice_bytes(in.g.width, in.g.depth);
             if (slice == 0 || slice > optin) return cudaErrorInvalidConfiguration;
         }
         job.letters = in.letters ? 1 : 0;

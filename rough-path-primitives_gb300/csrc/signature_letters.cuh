@@ -769,14 +769,15 @@ __device__ __forceinline__ void letter_reverse_step_family(float* region, const 
     letter_cotangent_lower<W, D, D - 3>(region, x1, glo, pinv, xa, c, lane);
 }
 
-// The reverse loop of one path by warp c: increments from the last (lane
-// a < W loads letter a four steps ahead), `step(xb, xa)` per increment, the
-// warp's letter partials per step into pbuf, and once per 8 steps (and at
-// the end) one CTA barrier after which threads t < 8 W add the W warps'
-// partials in warp order into the gradient rows.
-template <int W, int D, typename Step>
-__device__ __forceinline__ void letter_reverse_loop(const float* __restrict__ incr, int64_t off, int64_t len,
-                                                    float* grad, float* region, float* pbuf, uint32_t c,
+// The reverse loop of one path by warp c of team `tm` (the CTA, or a team of
+// W warps of the grouped launch): increments from the last (lane a < W loads
+// letter a four steps ahead), `step(xb, xa)` per increment, the warp's letter
+// partials per step into pbuf, and once per 8 steps (and at the end) one team
+// barrier after which ranks t < 8 W add the W warps' partials in warp order
+// into the gradient rows.
+template <int W, int D, typename Team, typename Step>
+__device__ __forceinline__ void letter_reverse_loop(const Team& tm, const float* __restrict__ incr, int64_t off,
+                                                    int64_t len, float* grad, float* region, float* pbuf, uint32_t c,
                                                     uint32_t lane, Step&& step) {
     using F = LetterLayout<W, D>;
     using Rev = LetterRevLayout<W, D>;
@@ -817,8 +818,8 @@ __device__ __forceinline__ void letter_reverse_loop(const float* __restrict__ in
             if (slot == NB - 1 || i == len - 1) {
                 // the block's gradient rows: the W warps' partials added in
                 // warp order (the other half of pbuf takes the next block)
-                __syncthreads();
-                const uint32_t t = threadIdx.x;
+                tm.sync();
+                const uint32_t t = tm.rank();
                 if (t < (slot + 1) * W) {
                     const uint32_t st = t / W, a = t % W;
                     float v = 0.0f;
@@ -831,18 +832,19 @@ __device__ __forceinline__ void letter_reverse_loop(const float* __restrict__ in
     }
 }
 
-// Forward and reverse pass of one path by warp c (k_signature_letters_rev).
-// Modes: kForward | kBackward [| kTopLevel] (the forward pass first, writing
-// the signature row with kTopLevel) and kBackward | kLoadFinal (the final
-// signature read from sig).  `pbuf` is the CTA's partials buffer
+// Forward and reverse pass of one path by warp c of team `tm` (the CTA in
+// k_signature_letters_rev, a team of W warps in the grouped launch).  Modes:
+// kForward | kBackward [| kTopLevel] (the forward pass first, writing the
+// signature row with kTopLevel) and kBackward | kLoadFinal (the final
+// signature read from sig).  `pbuf` is the team's partials buffer
 // (LetterRevLayout::pbuf_floats), `region` the warp's shared memory
-// (LetterRevLayout::warp_floats).  Contains CTA barriers: every warp of the
-// CTA runs the same path.
-template <int W, int D>
-__device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, int64_t b, int64_t off, int64_t len,
-                                               float* sig, int64_t sig_stride, const float* __restrict__ seed,
-                                               int64_t seed_stride, float* grad, int mode, float* region,
-                                               float* pbuf, uint32_t c, uint32_t lane) {
+// (LetterRevLayout::warp_floats).  Contains team barriers: every warp of the
+// team runs the same path.
+template <int W, int D, typename Team>
+__device__ __forceinline__ void letter_fwd_bwd(const Team& tm, const float* __restrict__ incr, int64_t b, int64_t off,
+                                               int64_t len, float* sig, int64_t sig_stride,
+                                               const float* __restrict__ seed, int64_t seed_stride, float* grad,
+                                               int mode, float* region, float* pbuf, uint32_t c, uint32_t lane) {
     using F = LetterLayout<W, D>;
     using Rev = LetterRevLayout<W, D>;
     constexpr int R = F::rows_per_lane;
@@ -913,7 +915,7 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
                 gtop[a][e] = fl ? sdr[level_start<W>(D) + c * F::slice(D) + (u * W + a) * W + e] : 0.0f;
         }
         float gf = fl ? sdr[level_start<W>(D - 2) + c * F::slice(D - 2) + u] : 0.0f;
-        letter_reverse_loop<W, D>(incr, off, len, grad, region, pbuf, c, lane, [&](const float* xb, float(&xa)[W]) {
+        letter_reverse_loop<W, D>(tm, incr, off, len, grad, region, pbuf, c, lane, [&](const float* xb, float(&xa)[W]) {
             letter_reverse_step_family<W, D>(region, xb, gtop, sdf, gdf, sf, gf, slo, glo, pinv, xa, c, lane);
         });
     } else {
@@ -927,7 +929,7 @@ __device__ __forceinline__ void letter_fwd_bwd(const float* __restrict__ incr, i
             for (int a = 0; a < W; ++a)
                 gtop[q][a] = row ? sdr[level_start<W>(D) + c * F::slice(D) + p * W + a] : 0.0f;
         }
-        letter_reverse_loop<W, D>(incr, off, len, grad, region, pbuf, c, lane, [&](const float* xb, float(&xa)[W]) {
+        letter_reverse_loop<W, D>(tm, incr, off, len, grad, region, pbuf, c, lane, [&](const float* xb, float(&xa)[W]) {
             letter_reverse_step<W, D>(region, xb, gtop, sd, gd, slo, glo, pinv, xa, c, lane);
         });
     }

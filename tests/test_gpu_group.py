@@ -78,7 +78,8 @@ def run_group_and_separate(orc, jobs, schedule=0):
     for j, a in zip(jobs, grouped):
         check_oracle(orc, j, a)
         alone = device_args(j)
-        separate(j, alone, j["threads"] | (schedule & (1 << 27)))
+        # a letter job (threads 0) against its kernel's explicit schedule
+        separate(j, alone, (j["threads"] or (32 | (1 << 16))) | (schedule & (1 << 27)))
         torch.cuda.synchronize()
         for got, want in zip(a[2:], alone[2:]):
             if got is not None:
@@ -108,6 +109,21 @@ def test_cotangent_workspace_jobs(orc):
             make_job(rng, 3, 4, 50, torch.float64, ragged=(0, 30), threads=128 | cot)]
     run_group_and_separate(orc, jobs)
     run_group_and_separate(orc, jobs, schedule=640 | (1 << 27))
+
+
+def test_fp32_forward_reverse_jobs_take_letter_warps(orc):
+    """FP32 forward + reverse jobs of an instantiated shape (depth >= 3) with
+    threads = 0 run the warp-per-letter forward + reverse code inside the
+    group (a team of W warps meeting on its named barrier for the letter
+    gradients): outputs equal a separate call of that kernel bit for bit and
+    the FP64 oracle within 1e-5; the family form (W5 D5), the row form (W8
+    D4, ragged with empty paths), gradient-only (W3 D6), beside an FP64 job."""
+    rng = np.random.default_rng(59)
+    jobs = [make_job(rng, 5, 5, 12, torch.float32, L=20),
+            make_job(rng, 8, 4, 30, torch.float32, ragged=(0, 30)),
+            make_job(rng, 3, 6, 10, torch.float32, L=11, sig=False),
+            make_job(rng, 5, 5, 9, torch.float64, L=13, threads=128)]
+    run_group_and_separate(orc, jobs)
 
 
 def test_fp64_and_fp32_ragged_forward(orc):
