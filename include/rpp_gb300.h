@@ -460,7 +460,9 @@ int rpp_gb_signature_with_schedule(const rpp_gb_plan* plan, rpp_gb_stream stream
  * so one launch covers batches of different (width, depth) and of FP64 and
  * FP32 together, e.g. inside one captured CUDA graph.  Each path of job j is
  * run by a team of `threads` threads (bits 0-9: a multiple of 32, at least
- * width*depth; 0: the CTA size of the schedule recorded for that shape by
+ * width*depth; 0: for FP32 jobs of the shapes of the warp-per-letter kernels
+ * (rpp_gb_signature_tune's bit 16) a team of width warps running that code,
+ * otherwise the CTA size of the schedule recorded for that shape by
  * rpp_gb_signature_tune, else a heuristic; bit 26, or a recorded one-launch
  * schedule with bit 26, on an FP64 forward + reverse job: its cotangent level
  * and chains in a stream-ordered global workspace, one slice per team, so
