@@ -2,7 +2,7 @@
 (rpp_gb_signature_group): each job's outputs against the oracle and, bit for
 bit, against a separate rpp_gb_signature call whose CTA size is the job's team
 size (the team size fixes the order in which the letter gradients' partial
-sums are added), the two mixed workloads of the survey's configurations at
+sums are added), the two mixed workloads of the benchmark configurations at
 test size, several teams per CTA, a CUDA graph replay, and the refusals."""
 import importlib
 
